@@ -1,0 +1,346 @@
+#!/usr/bin/env python
+"""Benchmark: vectorized NUTS on covtype-shaped Bayesian logistic regression.
+
+Workload (1 GPU): N=581,012 rows x D=55 (10 continuous + 44 binary + intercept),
+1024 chains, prior N(0,1), synthetic seeded data; NUTS with Stan warmup
+(500 iterations, untimed setup), then W warm-up steps and K timed steps.  A
+"step" is one sampling block of ``--iters-per-step`` NUTS transitions for all
+chains.  value = min over the 55 coefficients of bulk-ESS (rank-normalised
+split-ESS) of the draws of the timed steps / timed seconds; grad evals/s is
+reported beside it.  L2 is flushed (a 512 MB write) before every timed step.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+"""
+import argparse
+import ctypes
+import json
+import os
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "min bulk-ESS/s & grad evals/s: fused vs plain NUTS on 1 GB300 at R-hat<1.01"
+WORKLOAD = "logreg-covtype-shaped N=581012 D=55, 1024 chains, NUTS max_tree_depth=10, 500 warmup"
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--engine", default="fused", choices=["fused", "plain"])
+    p.add_argument("--precision", default=None, choices=["fp32", "bf16x3"])
+    p.add_argument("--chains", type=int, default=1024)
+    p.add_argument("--n", type=int, default=581012)
+    p.add_argument("--num-warmup", type=int, default=500)
+    p.add_argument("--iters-per-step", type=int, default=10)
+    p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--cpu-seconds", type=float, default=20.0)
+    return p.parse_args()
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        d = json.load(open(path))
+        return d.get("bf16_tflops", 1900.0), d.get("bf16_tflops_sustained", 1700.0), d.get("hbm_gbs", 6800.0), \
+            "measured"
+    return 1900.0, 1700.0, 6800.0, "fallback"
+
+
+class Clocks:
+    """Samples nvidia-smi clocks/throttle reasons during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu):
+        self.gpu = gpu
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", "clocks_bench.csv")
+
+    def start(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                         stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        self.proc.wait()
+        self.f.close()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        med = float(np.median(sm)) if sm else None
+        return {"sm_mhz": med, "sm_max_mhz": smax, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def min_bulk_ess(z):
+    from numpyro_gb300.diagnostics import bulk_effective_sample_size, split_gelman_rubin
+
+    ess = np.array([bulk_effective_sample_size(z[..., d]) for d in range(z.shape[-1])])
+    rhat = np.array([split_gelman_rubin(z[..., d]) for d in range(z.shape[-1])])
+    return float(ess.min()), float(np.max(rhat))
+
+
+def cpu_baseline(X, y, chains, seconds, prec="fp32"):
+    """Times the C oracle (OpenMP over chains) on a bounded sample of the workload."""
+    from oracle import build_oracle
+
+    lib = build_oracle.load(prec)
+    cores = len(os.sched_getaffinity(0))
+    res = build_oracle.run_logreg(lib, X, y, chains=chains, num_warmup=50, num_samples=40, seed=0,
+                                  threads=cores, budget_s=seconds)
+    from numpyro_gb300.diagnostics import bulk_effective_sample_size
+
+    z = res["samples"]
+    ess = min(bulk_effective_sample_size(z[..., d]) for d in range(z.shape[-1]))
+    return {
+        "value": ess / res["sampling_s"],
+        "unit": "ESS/s",
+        "cores": res["threads"],
+        "kind": "port",
+        "grad_evals_per_s": res["sampling_grad_evals"] / res["sampling_s"],
+        "sample": "%d chains x (50 warmup + 40 samples) NUTS on the full N=%d x %d data, %s C oracle; "
+                  "ESS/s = min bulk-ESS of the 40 draws/chain / sampling seconds" % (
+                      res["chains"], X.shape[0], X.shape[1], prec),
+    }
+
+
+def run_reference(args):
+    """--impl reference: the oracle port of numpyro's NUTS on the host cores."""
+    from numpyro_gb300 import datasets
+
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    X, y, _ = datasets.covtype_like(seed=0, n=args.n)
+    steps = []
+    cb = None
+    for k in range(args.warmup + args.steps):
+        cb = cpu_baseline(X, y, chains=min(16, len(os.sched_getaffinity(0))), seconds=args.cpu_seconds)
+        if k >= args.warmup:
+            steps.append(cb)
+    value = float(np.mean([s["value"] for s in steps]))
+    line = {"metric": METRIC, "value": value, "unit": "ESS/s", "impl": "reference", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "dtype": "f32",
+            "data": "synthetic", "config": {"workload": WORKLOAD, "chains_timed": cb["cores"]},
+            "cpu_baseline": {**cb, "value": value},
+            "e2e": {"value": value, "unit": "ESS/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "grad_evals_per_s": float(np.mean([s["grad_evals_per_s"] for s in steps])),
+            "vs_baseline": None}
+    print(json.dumps(line))
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    import torch
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    from numpyro_gb300 import NUTS, datasets, models
+
+    precision = args.precision or ("bf16x3" if _tc_available() else "fp32")
+    X, y, _ = datasets.covtype_like(seed=0, n=args.n)
+    model = models.LogisticRegression(X, y)
+    C = args.chains
+    kernel = NUTS(model, num_chains=C, engine=args.engine, precision=precision)
+    seed = 1000 + rank  # replicas: independent chains per rank
+    t0 = time.perf_counter()
+    state = kernel.init(seed, args.num_warmup)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record()
+    kernel.run_device(state, args.num_warmup, collect_start=args.num_warmup, collect=())
+    ev1.record()
+    torch.cuda.synchronize()
+    warmup_ms = ev0.elapsed_time(ev1)
+    B = args.iters_per_step
+    flush = torch.empty(128 * 1024 * 1024, dtype=torch.float32, device="cuda")
+    for _ in range(args.warmup):
+        kernel.run_device(state, B, collect=())
+    torch.cuda.synchronize()
+    # ---------------- timed region (device-resident inputs)
+    clocks = Clocks(local)
+    clocks.start()
+    ticks0 = kernel.stats()["ticks"]
+    zs, nsteps, step_ms = [], [], []
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    for _ in range(args.steps):
+        flush.fill_(1.0)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        out = kernel.run_device(state, B, collect=("z", "num_steps"))
+        b.record()
+        zs.append(out["z"])
+        nsteps.append(out["num_steps"])
+        b.synchronize()
+        step_ms.append(a.elapsed_time(b))
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    ticks = kernel.stats()["ticks"] - ticks0
+    clk = clocks.stop()
+    total_ms = float(sum(step_ms))
+    z = torch.cat(zs, dim=1).cpu().numpy()
+    grad_evals = int(torch.cat(nsteps, dim=1).sum().item())
+    ess, rhat = min_bulk_ess(z)
+    if dist:
+        t = torch.tensor([total_ms, ess, grad_evals], dtype=torch.float64, device="cuda")
+        tmax = t.clone()
+        dist.all_reduce(tmax, op=dist.ReduceOp.MAX)
+        dist.all_reduce(t, op=dist.ReduceOp.SUM)
+        total_ms, ess, grad_evals = float(tmax[0]), float(t[1]), int(t[2])
+    value = ess / (total_ms / 1e3)
+    # ---------------- dominant kernel: the potential, timed alone on the same stream
+    pot_ms = _time_potential(kernel, state, reps=10)
+    burst, sustained, hbm, peak_kind = measured_peaks()
+    flop = 4.0 * X.shape[0] * X.shape[1] * C
+    achieved = flop / (pot_ms / 1e3) / 1e12
+    roofline = {"bound": "tensor", "achieved": achieved, "peak": burst, "unit": "TFLOP/s",
+                "frac": achieved / burst, "traffic": None, "peak_kind": peak_kind + " burst bf16",
+                "kernel": "logreg potential (%s)" % precision, "algorithmic_flop_per_launch": flop,
+                "launch_ms": pot_ms}
+    # ---------------- end to end through the public API with host buffers
+    e2e = None
+    if not args.no_e2e:
+        e2e = _e2e(kernel, state, args.steps, B)
+    line = {
+        "metric": METRIC, "value": value, "unit": "ESS/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": total_ms / max(1, args.steps), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "bf16x3" if precision == "bf16x3" else "f32",
+        "data": "synthetic", "impl": "ours",
+        "config": {"workload": WORKLOAD, "chains": C, "n": X.shape[0], "d": X.shape[1], "engine": args.engine,
+                   "precision": precision, "iters_per_step": B, "l2": "flushed (512 MB write) before each step",
+                   "parallelism": "replicas" if world > 1 else "single"},
+        "grad_evals_per_s": grad_evals / (total_ms / 1e3),
+        "min_bulk_ess": ess, "rhat_max": rhat, "warmup_s": warmup_ms / 1e3,
+        "setup_s": time.perf_counter() - t0,
+        "roofline": roofline, "clocks": clk, "gpu_launches": int(ticks * _launches_per_tick(precision)),
+        "e2e": e2e,
+    }
+    if rank == 0 and not args.no_cpu and world == 1:
+        try:
+            line["cpu_baseline"] = cpu_baseline(X, y, chains=min(16, len(os.sched_getaffinity(0))),
+                                                seconds=args.cpu_seconds)
+        except Exception as ex:  # the baseline is reported, never required for the GPU number
+            line["cpu_baseline"] = {"value": None, "error": str(ex)[:200]}
+    if rank == 0:
+        print(json.dumps(line))
+    if dist:
+        dist.destroy_process_group()
+    kernel.close()
+    return 0
+
+
+def _tc_available():
+    try:
+        from numpyro_gb300 import _lib
+
+        return bool(getattr(_lib.load(), "gbn_tc_available", lambda: 0)())
+    except Exception:
+        return False
+
+
+def _launches_per_tick(precision):
+    return 2 if precision == "bf16x3" else 3  # advance + potential kernels
+
+
+def _time_potential(kernel, state, reps=10):
+    import torch
+
+    z = state.z.clone()
+    kernel.potential_and_grad(z)
+    torch.cuda.synchronize()
+    ts = []
+    for _ in range(reps):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        kernel.potential_and_grad(z)
+        b.record()
+        b.synchronize()
+        ts.append(a.elapsed_time(b))
+    return float(np.median(ts))
+
+
+def _e2e(kernel, state, steps, B):
+    """Same metric through the public API with host-resident state: every step
+    copies the chain state host->device, runs B transitions, and copies the
+    draws and state back."""
+    import torch
+
+    host = {}
+
+    def leaves(st):
+        a = st.adapt_state
+        return [st.i, st.z, st.z_grad, st.potential_energy, st.energy, st.num_steps, st.accept_prob,
+                st.mean_accept_prob, st.diverging, a.step_size, a.inverse_mass_matrix, a.mass_matrix_sqrt,
+                a.mass_matrix_sqrt_inv, a.ss_state, a.mm_state[0], a.mm_state[1], a.mm_state[2], a.window_idx,
+                st.rng_key]
+
+    dev = leaves(state)
+    host = [t.cpu().pin_memory() for t in dev]
+    h2d = sum(t.numel() * t.element_size() for t in host)
+    zs = []
+    d2h = 0
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    a.record()
+    for _ in range(steps):
+        for d, h in zip(dev, host):
+            d.copy_(h, non_blocking=True)
+        out = kernel.run_device(state, B, collect=("z", "num_steps"))
+        zh = torch.empty(out["z"].shape, dtype=out["z"].dtype, pin_memory=True)
+        zh.copy_(out["z"], non_blocking=True)
+        for d, h in zip(dev, host):
+            h.copy_(d, non_blocking=True)
+        zs.append(zh)
+        d2h = zh.numel() * 4 + h2d
+    b.record()
+    torch.cuda.synchronize()
+    ms = a.elapsed_time(b)
+    z = torch.cat(zs, dim=1).numpy()
+    ess, _ = min_bulk_ess(z)
+    return {"value": ess / (ms / 1e3), "unit": "ESS/s", "h2d_bytes_per_step": int(h2d),
+            "d2h_bytes_per_step": int(d2h), "ms_per_step": ms / steps}
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,175 @@
+/*
+ * gbnuts.h -- C ABI of the GB300-native NUTS/HMC engine (libgbnuts.so).
+ *
+ * The library replaces the device arithmetic of numpyro's vectorized-chain
+ * NUTS/HMC transition.  Each entry point below names the reference interface
+ * it stands in for (paths relative to the numpyro source tree):
+ *
+ *   gbn_create / gbn_destroy      NUTS.__init__ / HMC.__init__        numpyro/infer/hmc.py:625-686, :916-951
+ *                                 (model = registry family + data; potential_energy numpyro/infer/util.py:333-358)
+ *   gbn_init                      HMC.init (vmapped hmc_init_fn)      numpyro/infer/hmc.py:740-799, init_kernel :193-362,
+ *                                 find_valid_initial_params           numpyro/infer/util.py:366-508
+ *   gbn_sample                    HMC.sample (vmapped sample_kernel)  numpyro/infer/hmc.py:806-816, :459-530
+ *   gbn_run                       MCMC.run, chain_method="vectorized" numpyro/infer/mcmc.py:635-729 with fori_collect
+ *                                 numpyro/util.py:321-454 (whole warmup+sampling loop on the device)
+ *   gbn_potential_and_grad        value_and_grad(potential_fn)        numpyro/infer/hmc_util.py:242-252
+ *   gbn_potential_vjp             jax.vjp of potential_fn (adjoint)   numpyro/infer/hmc_util.py:242-252
+ *   gbn_last_error                RuntimeError text of init failure   numpyro/infer/util.py:800-832
+ *
+ * Conventions: every entry point is extern "C", returns an int status
+ * (GBN_OK = 0), never throws, and never synchronises the caller's stream
+ * except where documented (gbn_init and gbn_run poll a device counter).
+ * Pointers named d_* are device pointers owned by the caller; the library
+ * owns its model data and scratch inside the handle.  Handles are not
+ * thread-safe; distinct handles are independent.
+ */
+#ifndef GBNUTS_H
+#define GBNUTS_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GBN_ABI_VERSION 1
+
+/* status codes */
+#define GBN_OK 0
+#define GBN_ERR_INVALID_ARG 1
+#define GBN_ERR_SHAPE 2
+#define GBN_ERR_CUDA 3
+#define GBN_ERR_TIMEOUT 4      /* tick budget exhausted / device wait gave up */
+#define GBN_ERR_INIT_FAILED 5  /* no finite potential after 100 init attempts */
+#define GBN_ERR_UNSUPPORTED 6
+#define GBN_ERR_OOM 7
+
+/* model families (the potential registry) */
+#define GBN_FAMILY_HIER_NC 1   /* non-centred hierarchical normal, many datasets  */
+#define GBN_FAMILY_LOGREG 2    /* Bernoulli-logit GLM, Normal(0,1) prior          */
+#define GBN_FAMILY_HORSESHOE 3 /* Gaussian GLM, horseshoe prior                   */
+#define GBN_FAMILY_SV 4        /* Gaussian random walk + StudentT volatility      */
+
+/* engines */
+#define GBN_ENGINE_FUSED 0 /* per-chain trees, no lock-step, fused/tensor-core potentials */
+#define GBN_ENGINE_PLAIN 1 /* lock-step masked trees (numpyro vmap semantics), FP32 CUDA-core potentials */
+
+/* algorithms */
+#define GBN_ALGO_NUTS 0
+#define GBN_ALGO_HMC 1
+
+/* potential precision (logistic family) */
+#define GBN_PREC_FP32 0   /* FP32 CUDA cores */
+#define GBN_PREC_BF16X3 1 /* tcgen05 BF16 split precision, FP32 accumulate */
+
+typedef struct gbn_handle_s* gbn_handle;
+
+/* Model description; host pointers, copied to the device by gbn_create. */
+typedef struct {
+  int32_t family;
+  int32_t num_models; /* HIER_NC: number of independent datasets; else 1 */
+  int64_t n;          /* rows (LOGREG/HORSESHOE), total groups (HIER_NC), T (SV) */
+  int32_t p;          /* features (LOGREG/HORSESHOE); unused otherwise */
+  const float* x;     /* [n][p] row-major design matrix (LOGREG, HORSESHOE) */
+  const float* y;     /* [n] responses / observations / returns */
+  const float* sigma; /* [n] observation sd (HIER_NC) */
+  const int32_t* offsets; /* [num_models+1] group offsets (HIER_NC) */
+  double hyper[8];    /* prior hyper-parameters, family specific (see models.py) */
+} gbn_model_desc;
+
+/* Kernel configuration: numpyro NUTS/HMC constructor arguments. */
+typedef struct {
+  int32_t num_chains;
+  int32_t chains_per_model; /* HIER_NC: chain c runs dataset c / chains_per_model */
+  int32_t algo;
+  int32_t engine;
+  int32_t precision;
+  int32_t max_tree_depth_warmup; /* max_tree_depth (d1, d2) */
+  int32_t max_tree_depth;
+  int32_t adapt_step_size;
+  int32_t adapt_mass_matrix;
+  int32_t dense_mass; /* only 0 is supported by this build */
+  int32_t regularize_mass_matrix;
+  int32_t find_heuristic_step_size;
+  int32_t num_steps; /* HMC: fixed number of steps, 0 = from trajectory_length */
+  double target_accept_prob;
+  double trajectory_length; /* HMC */
+  double max_delta_energy;  /* 1000 */
+  double init_step_size;
+  uint64_t seed;
+} gbn_config;
+
+/* HMCState (numpyro/infer/hmc.py:31-47) + HMCAdaptState (hmc_util.py:18-30)
+ * as caller-owned device buffers, chain-major.  C = num_chains, D = latent dim. */
+typedef struct {
+  int32_t* i;                   /* [C] iteration */
+  float* z;                     /* [C][D] unconstrained position */
+  float* z_grad;                /* [C][D] */
+  double* potential_energy;     /* [C] */
+  double* energy;               /* [C] */
+  int32_t* num_steps;           /* [C] leapfrog steps of the last trajectory */
+  float* accept_prob;           /* [C] */
+  float* mean_accept_prob;      /* [C] */
+  uint8_t* diverging;           /* [C] */
+  float* step_size;             /* [C] adapt_state.step_size */
+  float* inverse_mass_matrix;   /* [C][D] diagonal */
+  float* mass_matrix_sqrt;      /* [C][D] */
+  float* mass_matrix_sqrt_inv;  /* [C][D] */
+  double* ss_state;             /* [C][5] dual averaging (x_t, x_avg, g_avg, t, prox_center) */
+  double* mm_mean;              /* [C][D] Welford mean */
+  double* mm_m2;                /* [C][D] Welford m2 */
+  int32_t* mm_n;                /* [C] */
+  int32_t* window_idx;          /* [C] */
+  uint32_t* rng_key;            /* [C][2] (chain id, transition counter) */
+} gbn_state;
+
+/* Per-iteration collection buffers for gbn_run (any pointer may be NULL). */
+typedef struct {
+  float* samples;          /* [C][S][D] z (unconstrained) */
+  int32_t* num_steps;      /* [C][S] */
+  float* accept_prob;      /* [C][S] */
+  uint8_t* diverging;      /* [C][S] */
+  double* potential_energy;/* [C][S] */
+  float* step_size;        /* [C][S] */
+} gbn_collect;
+
+typedef struct {
+  int64_t ticks;          /* device ticks (one leapfrog for every pending chain) */
+  int64_t grad_evals;     /* gradient evaluations consumed by chains */
+  int64_t potential_launches;
+  double device_ms;       /* CUDA-event time of the last gbn_run/gbn_sample */
+} gbn_stats;
+
+int gbn_abi_version(void);
+const char* gbn_last_error(gbn_handle h); /* h may be NULL: last global error */
+
+int gbn_create(gbn_handle* out, const gbn_model_desc* model, const gbn_config* cfg);
+int gbn_destroy(gbn_handle h);
+int gbn_latent_dim(gbn_handle h, int32_t* dim);
+
+/* U(z) and dU/dz for num_points latent vectors (device pointers). */
+int gbn_potential_and_grad(gbn_handle h, void* stream, const float* d_z, int32_t num_points,
+                           double* d_pe, float* d_grad);
+/* Vector-Jacobian product of U: d_out = cot[k] * dU/dz(z_k). */
+int gbn_potential_vjp(gbn_handle h, void* stream, const float* d_z, int32_t num_points,
+                      const double* d_cot, float* d_out);
+
+/* Initialise every chain: init_to_uniform(radius=2) when d_init_z is NULL,
+ * validity retries, initial adaptation state. */
+int gbn_init(gbn_handle h, void* stream, int32_t num_warmup, const float* d_init_z,
+             const float* d_inverse_mass_matrix, gbn_state* st);
+
+/* One transition for every chain (MCMCKernel.sample). */
+int gbn_sample(gbn_handle h, void* stream, gbn_state* st);
+
+/* num_iterations transitions per chain; iteration j (0-based, this call) is
+ * collected when j >= collect_start and (j - collect_start) % thinning == 0. */
+int gbn_run(gbn_handle h, void* stream, gbn_state* st, int32_t num_iterations,
+            int32_t collect_start, int32_t thinning, gbn_collect* out);
+
+int gbn_get_stats(gbn_handle h, gbn_stats* stats);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GBNUTS_H */

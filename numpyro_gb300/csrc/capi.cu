@@ -1,0 +1,513 @@
+// capi.cu -- the extern "C" boundary of libgbnuts (declared in include/gbnuts.h).
+//
+// Host-side engine: owns the model data and tree scratch, builds the Stan
+// adaptation schedule (numpyro/infer/hmc_util.py:387-436), runs the
+// validity-retrying initialisation (numpyro/infer/util.py:366-508) and drives
+// the advance/potential "ticks" until every chain has finished the requested
+// transitions.  No exception crosses the ABI; every entry point returns a
+// status and records a message readable through gbn_last_error.
+#include <cmath>
+#include <cstdio>
+#include <algorithm>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/gbnuts.h"
+#include "common.cuh"
+#include "internal.h"
+
+using namespace gbn;
+
+struct gbn_handle_s {
+  gbn_config cfg{};
+  ModelDev m;
+  int C = 0, D = 0, maxd = 1;
+  EngineBufs e{};
+  AdvParams hp{};
+  AdvParams* dP = nullptr;
+  int32_t* counters = nullptr;
+  int32_t* h_counters = nullptr;  // pinned
+  int32_t* done_count = nullptr;
+  int done_cap = 0;
+  int32_t* flags = nullptr;
+  int32_t* err_word = nullptr;
+  int32_t* window_end = nullptr;
+  int num_windows = 0;
+  int num_warmup = 0;
+  int initialised = 0;
+  std::string err;
+  gbn_stats stats{};
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  std::vector<void*> allocs;
+};
+
+static thread_local std::string g_last_error;
+
+static int fail(gbn_handle h, int code, const std::string& msg) {
+  g_last_error = msg;
+  if (h) h->err = msg;
+  return code;
+}
+
+static int cuda_fail(gbn_handle h, cudaError_t e, const char* what) {
+  std::string msg = std::string(what) + ": " + cudaGetErrorString(e);
+  return fail(h, GBN_ERR_CUDA, msg);
+}
+
+template <typename T>
+static cudaError_t dalloc(gbn_handle h, T** p, size_t count) {
+  if (count == 0) count = 1;
+  cudaError_t e = cudaMalloc((void**)p, sizeof(T) * count);
+  if (e == cudaSuccess) {
+    h->allocs.push_back((void*)*p);
+    cudaMemset(*p, 0, sizeof(T) * count);
+  }
+  return e;
+}
+
+// Stan windows, numpyro/infer/hmc_util.py:387-436
+static std::vector<int> adaptation_window_ends(int num_steps) {
+  std::vector<int> ends;
+  if (num_steps <= 0) return ends;
+  if (num_steps < 20) {
+    ends.push_back(num_steps - 1);
+    return ends;
+  }
+  int start_buffer = 75, end_buffer = 50, init_window = 25;
+  if (start_buffer + end_buffer + init_window > num_steps) {
+    start_buffer = (int)(0.15 * num_steps);
+    end_buffer = (int)(0.1 * num_steps);
+    init_window = num_steps - start_buffer - end_buffer;
+  }
+  ends.push_back(start_buffer - 1);
+  int end_window_start = num_steps - end_buffer;
+  int next_size = init_window, next_start = start_buffer;
+  while (next_start < end_window_start) {
+    int cur_start = next_start, cur_size = next_size;
+    if (3 * cur_size <= end_window_start - cur_start)
+      next_size = 2 * cur_size;
+    else
+      cur_size = end_window_start - cur_start;
+    next_start = cur_start + cur_size;
+    ends.push_back(next_start - 1);
+  }
+  ends.push_back(num_steps - 1);
+  return ends;
+}
+
+static void fill_state(AdvParams& P, const gbn_state* st) {
+  P.s.i = st->i;
+  P.s.z = st->z;
+  P.s.z_grad = st->z_grad;
+  P.s.potential_energy = st->potential_energy;
+  P.s.energy = st->energy;
+  P.s.num_steps = st->num_steps;
+  P.s.accept_prob = st->accept_prob;
+  P.s.mean_accept_prob = st->mean_accept_prob;
+  P.s.diverging = st->diverging;
+  P.s.step_size = st->step_size;
+  P.s.inverse_mass_matrix = st->inverse_mass_matrix;
+  P.s.mass_matrix_sqrt = st->mass_matrix_sqrt;
+  P.s.mass_matrix_sqrt_inv = st->mass_matrix_sqrt_inv;
+  P.s.ss_state = st->ss_state;
+  P.s.mm_mean = st->mm_mean;
+  P.s.mm_m2 = st->mm_m2;
+  P.s.mm_n = st->mm_n;
+  P.s.window_idx = st->window_idx;
+  P.s.rng_key = st->rng_key;
+}
+
+static bool state_ok(const gbn_state* st) {
+  return st && st->i && st->z && st->z_grad && st->potential_energy && st->energy && st->num_steps &&
+         st->accept_prob && st->mean_accept_prob && st->diverging && st->step_size && st->inverse_mass_matrix &&
+         st->mass_matrix_sqrt && st->mass_matrix_sqrt_inv && st->ss_state && st->mm_mean && st->mm_m2 &&
+         st->mm_n && st->window_idx && st->rng_key;
+}
+
+extern "C" {
+
+int gbn_abi_version(void) { return GBN_ABI_VERSION; }
+
+const char* gbn_last_error(gbn_handle h) { return h ? h->err.c_str() : g_last_error.c_str(); }
+
+int gbn_latent_dim(gbn_handle h, int32_t* dim) {
+  if (!h || !dim) return fail(h, GBN_ERR_INVALID_ARG, "gbn_latent_dim: null argument");
+  *dim = h->D;
+  return GBN_OK;
+}
+
+int gbn_destroy(gbn_handle h) {
+  if (!h) return GBN_OK;
+  cudaDeviceSynchronize();
+  if (h->m.tc) logreg_tc_free(h->m);
+  free_potential_scratch(h->m);
+  for (void* p : h->allocs) cudaFree(p);
+  if (h->h_counters) cudaFreeHost(h->h_counters);
+  if (h->ev0) cudaEventDestroy(h->ev0);
+  if (h->ev1) cudaEventDestroy(h->ev1);
+  delete h;
+  return GBN_OK;
+}
+
+int gbn_create(gbn_handle* out, const gbn_model_desc* md, const gbn_config* cfg) {
+  if (!out || !md || !cfg) return fail(nullptr, GBN_ERR_INVALID_ARG, "gbn_create: null argument");
+  *out = nullptr;
+  if (cfg->num_chains <= 0) return fail(nullptr, GBN_ERR_INVALID_ARG, "num_chains must be positive");
+  if (cfg->dense_mass) return fail(nullptr, GBN_ERR_UNSUPPORTED, "dense_mass=True is not supported by this engine");
+  if (cfg->algo != GBN_ALGO_NUTS && cfg->algo != GBN_ALGO_HMC)
+    return fail(nullptr, GBN_ERR_INVALID_ARG, "algo must be NUTS or HMC");
+  if (cfg->max_tree_depth < 1 || cfg->max_tree_depth > 20 || cfg->max_tree_depth_warmup < 1 ||
+      cfg->max_tree_depth_warmup > 20)
+    return fail(nullptr, GBN_ERR_INVALID_ARG, "max_tree_depth must be in [1, 20]");
+  if (cfg->algo == GBN_ALGO_HMC && cfg->num_steps <= 0 && !(cfg->trajectory_length > 0))
+    return fail(nullptr, GBN_ERR_INVALID_ARG, "HMC needs num_steps or trajectory_length");
+  gbn_handle h = new gbn_handle_s();
+  h->cfg = *cfg;
+  ModelDev& m = h->m;
+  m.family = md->family;
+  m.num_models = md->num_models > 0 ? md->num_models : 1;
+  m.n = md->n;
+  m.p = md->p;
+  m.precision = cfg->precision;
+  for (int k = 0; k < 8; ++k) m.hyper[k] = md->hyper[k];
+  int C = cfg->num_chains;
+  h->C = C;
+  std::vector<int32_t> chain_dim;
+  cudaError_t ce = cudaSuccess;
+  switch (m.family) {
+    case GBN_FAMILY_HIER_NC: {
+      if (!md->y || !md->sigma || !md->offsets || md->n <= 0) {
+        gbn_destroy(h);
+        return fail(nullptr, GBN_ERR_INVALID_ARG, "HIER_NC needs y, sigma, offsets");
+      }
+      int cpm = cfg->chains_per_model > 0 ? cfg->chains_per_model : C / m.num_models;
+      if (cpm * m.num_models != C) {
+        gbn_destroy(h);
+        return fail(nullptr, GBN_ERR_SHAPE, "num_chains must equal num_models * chains_per_model");
+      }
+      m.chains_per_model = cpm;
+      int Dmax = 0;
+      for (int k = 0; k < m.num_models; ++k) {
+        int J = md->offsets[k + 1] - md->offsets[k];
+        if (J < 0 || md->offsets[k + 1] > md->n) {
+          gbn_destroy(h);
+          return fail(nullptr, GBN_ERR_SHAPE, "HIER_NC offsets out of range");
+        }
+        Dmax = std::max(Dmax, J + 2);
+      }
+      m.D = Dmax;
+      chain_dim.resize(C);
+      for (int c = 0; c < C; ++c) {
+        int k = c / cpm;
+        chain_dim[c] = md->offsets[k + 1] - md->offsets[k] + 2;
+      }
+      if (m.hyper[0] <= 0) m.hyper[0] = 5.0;
+      if (m.hyper[1] <= 0) m.hyper[1] = 5.0;
+      ce = dalloc(h, &m.y, md->n);
+      if (ce == cudaSuccess) ce = dalloc(h, &m.sigma, md->n);
+      if (ce == cudaSuccess) ce = dalloc(h, &m.offsets, m.num_models + 1);
+      if (ce == cudaSuccess) ce = cudaMemcpy(m.y, md->y, sizeof(float) * md->n, cudaMemcpyHostToDevice);
+      if (ce == cudaSuccess) ce = cudaMemcpy(m.sigma, md->sigma, sizeof(float) * md->n, cudaMemcpyHostToDevice);
+      if (ce == cudaSuccess)
+        ce = cudaMemcpy(m.offsets, md->offsets, sizeof(int32_t) * (m.num_models + 1), cudaMemcpyHostToDevice);
+      break;
+    }
+    case GBN_FAMILY_LOGREG:
+    case GBN_FAMILY_HORSESHOE: {
+      if (!md->x || !md->y || md->n <= 0 || md->p <= 0) {
+        gbn_destroy(h);
+        return fail(nullptr, GBN_ERR_INVALID_ARG, "GLM families need x [n][p] and y [n]");
+      }
+      if (m.family == GBN_FAMILY_LOGREG && md->p > 64) {
+        gbn_destroy(h);
+        return fail(nullptr, GBN_ERR_UNSUPPORTED, "LOGREG supports p <= 64 features");
+      }
+      m.D = (m.family == GBN_FAMILY_LOGREG) ? md->p : 2 * md->p + 2;
+      if (m.family == GBN_FAMILY_LOGREG && m.hyper[0] <= 0) m.hyper[0] = 1.0;
+      size_t nx = (size_t)md->n * md->p;
+      ce = dalloc(h, &m.x, nx);
+      if (ce == cudaSuccess) ce = dalloc(h, &m.y, md->n);
+      if (ce == cudaSuccess) ce = cudaMemcpy(m.x, md->x, sizeof(float) * nx, cudaMemcpyHostToDevice);
+      if (ce == cudaSuccess) ce = cudaMemcpy(m.y, md->y, sizeof(float) * md->n, cudaMemcpyHostToDevice);
+      break;
+    }
+    case GBN_FAMILY_SV: {
+      if (!md->y || md->n <= 1) {
+        gbn_destroy(h);
+        return fail(nullptr, GBN_ERR_INVALID_ARG, "SV needs returns y [T], T >= 2");
+      }
+      m.D = (int)md->n + 2;
+      if (m.hyper[0] <= 0) m.hyper[0] = 10.0;
+      if (m.hyper[1] <= 0) m.hyper[1] = 0.1;
+      ce = dalloc(h, &m.y, md->n);
+      if (ce == cudaSuccess) ce = cudaMemcpy(m.y, md->y, sizeof(float) * md->n, cudaMemcpyHostToDevice);
+      break;
+    }
+    default:
+      gbn_destroy(h);
+      return fail(nullptr, GBN_ERR_UNSUPPORTED, "unknown model family");
+  }
+  if (ce != cudaSuccess) {
+    int r = cuda_fail(nullptr, ce, "gbn_create: model upload");
+    gbn_destroy(h);
+    return r;
+  }
+  int D = m.D;
+  h->D = D;
+  h->maxd = std::max(cfg->max_tree_depth, cfg->max_tree_depth_warmup);
+  size_t CD = (size_t)C * D;
+  EngineBufs& e = h->e;
+  float** vecs[] = {&e.z_l, &e.r_l, &e.g_l, &e.z_r, &e.r_r, &e.g_r, &e.z_p,
+                    &e.g_p, &e.z_sp, &e.g_sp, &e.rsum, &e.rsum_sub, &e.Q, &e.G};
+  for (float** v : vecs)
+    if (ce == cudaSuccess) ce = dalloc(h, v, CD);
+  if (ce == cudaSuccess) ce = dalloc(h, &e.r_ck, CD * h->maxd);
+  if (ce == cudaSuccess) ce = dalloc(h, &e.rs_ck, CD * h->maxd);
+  if (ce == cudaSuccess) ce = dalloc(h, &e.PE, (size_t)C);
+  if (ce == cudaSuccess) ce = dalloc(h, &e.ctl, (size_t)C);
+  if (ce == cudaSuccess && !chain_dim.empty()) {
+    ce = dalloc(h, &e.chain_dim, (size_t)C);
+    if (ce == cudaSuccess)
+      ce = cudaMemcpy(e.chain_dim, chain_dim.data(), sizeof(int32_t) * C, cudaMemcpyHostToDevice);
+  }
+  if (ce == cudaSuccess) ce = dalloc(h, &h->counters, 8);
+  if (ce == cudaSuccess) ce = dalloc(h, &h->flags, (size_t)C);
+  if (ce == cudaSuccess) ce = dalloc(h, &h->err_word, 4);
+  if (ce == cudaSuccess) ce = dalloc(h, &h->dP, 1);
+  if (ce == cudaSuccess) ce = cudaMallocHost((void**)&h->h_counters, sizeof(int32_t) * 8);
+  if (ce == cudaSuccess) ce = cudaEventCreate(&h->ev0);
+  if (ce == cudaSuccess) ce = cudaEventCreate(&h->ev1);
+  if (ce == cudaSuccess && m.family == GBN_FAMILY_LOGREG && m.precision == GBN_PREC_BF16X3) {
+    if (!logreg_tc_supported(m)) {
+      gbn_destroy(h);
+      return fail(nullptr, GBN_ERR_UNSUPPORTED, "bf16x3 tensor-core logistic path unavailable for this shape");
+    }
+    ce = logreg_tc_prepare(m, C);
+  }
+  if (ce == cudaSuccess) ce = ensure_potential_scratch(m, C);
+  if (ce != cudaSuccess) {
+    int r = cuda_fail(nullptr, ce, "gbn_create: allocation");
+    gbn_destroy(h);
+    return r == GBN_ERR_CUDA ? GBN_ERR_OOM : r;
+  }
+  // static parameters
+  AdvParams& P = h->hp;
+  P.e = e;
+  P.C = C;
+  P.D = D;
+  P.maxd = h->maxd;
+  P.mtd_warmup = cfg->max_tree_depth_warmup;
+  P.mtd = cfg->max_tree_depth;
+  P.algo = cfg->algo;
+  P.adapt_step = cfg->adapt_step_size;
+  P.adapt_mass = cfg->adapt_mass_matrix;
+  P.regularize = cfg->regularize_mass_matrix;
+  P.heuristic = cfg->find_heuristic_step_size;
+  P.lockstep = (cfg->engine == GBN_ENGINE_PLAIN);
+  P.fixed_steps = cfg->num_steps;
+  P.target_accept = (float)cfg->target_accept_prob;
+  P.max_dE = cfg->max_delta_energy > 0 ? cfg->max_delta_energy : 1000.0;
+  P.traj_len = cfg->trajectory_length;
+  P.seed.lo = (uint32_t)(cfg->seed & 0xffffffffu);
+  P.seed.hi = (uint32_t)(cfg->seed >> 32);
+  P.counters = h->counters;
+  P.error_word = h->err_word;
+  P.thinning = 1;
+  *out = h;
+  return GBN_OK;
+}
+
+int gbn_potential_and_grad(gbn_handle h, void* stream, const float* d_z, int32_t num_points, double* d_pe,
+                           float* d_grad) {
+  if (!h || !d_z || !d_pe || !d_grad || num_points <= 0)
+    return fail(h, GBN_ERR_INVALID_ARG, "gbn_potential_and_grad: bad argument");
+  cudaError_t e = launch_potential(h->m, d_z, num_points, d_pe, d_grad, nullptr, (cudaStream_t)stream);
+  if (e != cudaSuccess) return cuda_fail(h, e, "potential launch");
+  return GBN_OK;
+}
+
+int gbn_potential_vjp(gbn_handle h, void* stream, const float* d_z, int32_t num_points, const double* d_cot,
+                      float* d_out) {
+  if (!h || !d_z || !d_cot || !d_out || num_points <= 0)
+    return fail(h, GBN_ERR_INVALID_ARG, "gbn_potential_vjp: bad argument");
+  cudaStream_t st = (cudaStream_t)stream;
+  double* pe = nullptr;
+  cudaError_t e = cudaMallocAsync(&pe, sizeof(double) * num_points, st);
+  if (e != cudaSuccess) return cuda_fail(h, e, "vjp scratch");
+  e = launch_potential(h->m, d_z, num_points, pe, d_out, nullptr, st);
+  if (e == cudaSuccess) e = launch_scale_rows(d_cot, d_out, num_points, h->D, st);
+  cudaFreeAsync(pe, st);
+  if (e != cudaSuccess) return cuda_fail(h, e, "vjp launch");
+  return GBN_OK;
+}
+
+static cudaError_t upload_params(gbn_handle h, cudaStream_t st) {
+  return cudaMemcpyAsync(h->dP, &h->hp, sizeof(AdvParams), cudaMemcpyHostToDevice, st);
+}
+
+// Alternate advance/potential until no chain is active.  Returns GBN status.
+static int tick_loop(gbn_handle h, cudaStream_t st, int64_t max_ticks) {
+  int parity = 0;
+  int64_t ticks = 0;
+  const int batch = 16;
+  int64_t launches = 0;
+  for (;;) {
+    int last = 0;
+    for (int k = 0; k < batch; ++k) {
+      launch_advance(h->dP, h->C, h->D, parity, st);
+      cudaError_t e = launch_potential(h->m, h->e.Q, h->C, h->e.PE, h->e.G, h->counters + 2 * parity, st);
+      if (e != cudaSuccess) return cuda_fail(h, e, "tick launch");
+      last = parity;
+      parity ^= 1;
+      ++ticks;
+      ++launches;
+    }
+    cudaError_t e = cudaMemcpyAsync(h->h_counters, h->counters, sizeof(int32_t) * 4, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return cuda_fail(h, e, "tick loop");
+    if (h->h_counters[2 * last + 1] == 0) break;
+    if (ticks > max_ticks) return fail(h, GBN_ERR_TIMEOUT, "tick budget exhausted: chains did not finish");
+  }
+  h->stats.ticks += ticks;
+  h->stats.potential_launches += launches;
+  return GBN_OK;
+}
+
+int gbn_init(gbn_handle h, void* stream, int32_t num_warmup, const float* d_init_z, const float* d_inv_mass,
+             gbn_state* st) {
+  if (!h || !state_ok(st) || num_warmup < 0) return fail(h, GBN_ERR_INVALID_ARG, "gbn_init: bad argument");
+  cudaStream_t s = (cudaStream_t)stream;
+  h->num_warmup = num_warmup;
+  std::vector<int> ends = adaptation_window_ends(num_warmup);
+  if (ends.empty()) ends.push_back(-1);
+  h->num_windows = (int)ends.size();
+  if (h->window_end) {
+    cudaFree(h->window_end);
+    h->allocs.erase(std::find(h->allocs.begin(), h->allocs.end(), (void*)h->window_end));
+    h->window_end = nullptr;
+  }
+  cudaError_t e = dalloc(h, &h->window_end, ends.size());
+  if (e == cudaSuccess)
+    e = cudaMemcpy(h->window_end, ends.data(), sizeof(int32_t) * ends.size(), cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return cuda_fail(h, e, "gbn_init: schedule");
+  AdvParams& P = h->hp;
+  fill_state(P, st);
+  P.window_end = h->window_end;
+  P.num_windows = num_warmup > 0 ? h->num_windows : 0;
+  P.num_warmup = num_warmup;
+  P.col = CollectBufs{};
+  P.num_collect = 0;
+  P.collect_start = 0;
+  P.thinning = 1;
+  e = upload_params(h, s);
+  if (e != cudaSuccess) return cuda_fail(h, e, "gbn_init: params");
+  launch_set_rng_chain(st->rng_key, h->C, 0, s);
+  int C = h->C, D = h->D;
+  if (d_init_z) {
+    e = cudaMemcpyAsync(st->z, d_init_z, sizeof(float) * (size_t)C * D, cudaMemcpyDeviceToDevice, s);
+    if (e == cudaSuccess)
+      e = launch_potential(h->m, st->z, C, st->potential_energy, st->z_grad, nullptr, s);
+    if (e != cudaSuccess) return cuda_fail(h, e, "gbn_init: potential");
+  } else {
+    // find_valid_initial_params: up to 100 draws of init_to_uniform(radius=2)
+    launch_init_uniform(h->dP, C, D, 0, nullptr, s);
+    bool ok = false;
+    for (int attempt = 0; attempt < 100; ++attempt) {
+      e = launch_potential(h->m, st->z, C, st->potential_energy, st->z_grad, nullptr, s);
+      if (e == cudaSuccess) e = cudaMemsetAsync(h->counters + 6, 0, sizeof(int32_t), s);
+      if (e != cudaSuccess) return cuda_fail(h, e, "gbn_init: potential");
+      launch_check_valid(h->dP, C, h->flags, h->counters + 6, s);
+      e = cudaMemcpyAsync(h->h_counters + 6, h->counters + 6, sizeof(int32_t), cudaMemcpyDeviceToHost, s);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+      if (e != cudaSuccess) return cuda_fail(h, e, "gbn_init: validity");
+      if (h->h_counters[6] == 0) {
+        ok = true;
+        break;
+      }
+      launch_init_uniform(h->dP, C, D, attempt + 1, h->flags, s);
+    }
+    if (!ok)
+      return fail(h, GBN_ERR_INIT_FAILED,
+                  "Cannot find valid initial parameters. Please check your model again.");
+  }
+  launch_init_state(h->dP, C, D, d_inv_mass, (float)h->cfg.init_step_size, s);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(h, e, "gbn_init: state");
+  if (h->cfg.adapt_step_size && h->cfg.find_heuristic_step_size && num_warmup > 0) {
+    e = cudaMemsetAsync(h->counters, 0, sizeof(int32_t) * 4, s);
+    if (e != cudaSuccess) return cuda_fail(h, e, "gbn_init: counters");
+    launch_set_phase(h->dP, C, PH_HEUR_START, 0, s);
+    int r = tick_loop(h, s, 1 << 20);
+    if (r != GBN_OK) return r;
+  }
+  h->initialised = 1;
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(h, e, "gbn_init");
+  return GBN_OK;
+}
+
+int gbn_run(gbn_handle h, void* stream, gbn_state* st, int32_t num_iterations, int32_t collect_start,
+            int32_t thinning, gbn_collect* out) {
+  if (!h || !state_ok(st) || num_iterations < 0 || thinning < 1 || collect_start < 0)
+    return fail(h, GBN_ERR_INVALID_ARG, "gbn_run: bad argument");
+  if (!h->window_end) return fail(h, GBN_ERR_INVALID_ARG, "gbn_run: call gbn_init first");
+  if (num_iterations == 0) return GBN_OK;
+  cudaStream_t s = (cudaStream_t)stream;
+  AdvParams& P = h->hp;
+  fill_state(P, st);
+  P.col = CollectBufs{};
+  if (out) {
+    P.col.samples = out->samples;
+    P.col.num_steps = out->num_steps;
+    P.col.accept_prob = out->accept_prob;
+    P.col.diverging = out->diverging;
+    P.col.potential_energy = out->potential_energy;
+    P.col.step_size = out->step_size;
+  }
+  P.collect_start = collect_start;
+  P.thinning = thinning;
+  P.num_collect = (collect_start < num_iterations) ? (num_iterations - collect_start + thinning - 1) / thinning : 0;
+  if (!out) P.num_collect = 0;
+  cudaError_t e = cudaSuccess;
+  if (h->done_cap < num_iterations + 1) {
+    if (h->done_count) {
+      cudaFree(h->done_count);
+      h->allocs.erase(std::find(h->allocs.begin(), h->allocs.end(), (void*)h->done_count));
+    }
+    h->done_count = nullptr;
+    e = dalloc(h, &h->done_count, (size_t)num_iterations + 1);
+    if (e != cudaSuccess) return cuda_fail(h, e, "gbn_run: barrier counts");
+    h->done_cap = num_iterations + 1;
+  }
+  P.done_count = h->done_count;
+  e = upload_params(h, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(h->done_count, 0, sizeof(int32_t) * (num_iterations + 1), s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(h->counters, 0, sizeof(int32_t) * 4, s);
+  if (e != cudaSuccess) return cuda_fail(h, e, "gbn_run: setup");
+  launch_set_phase(h->dP, h->C, PH_START, num_iterations, s);
+  int64_t per_iter = (h->cfg.algo == GBN_ALGO_HMC) ? 4096 : ((int64_t)1 << h->maxd) + 8;
+  if (h->cfg.find_heuristic_step_size) per_iter += 512;
+  int64_t max_ticks = (int64_t)num_iterations * per_iter * (P.lockstep ? 2 : 1) + 4096;
+  cudaEventRecord(h->ev0, s);
+  int r = tick_loop(h, s, max_ticks);
+  cudaEventRecord(h->ev1, s);
+  if (r != GBN_OK) return r;
+  cudaEventSynchronize(h->ev1);
+  float ms = 0.0f;
+  cudaEventElapsedTime(&ms, h->ev0, h->ev1);
+  h->stats.device_ms = ms;
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(h, e, "gbn_run");
+  return GBN_OK;
+}
+
+int gbn_sample(gbn_handle h, void* stream, gbn_state* st) { return gbn_run(h, stream, st, 1, 0, 1, nullptr); }
+
+int gbn_get_stats(gbn_handle h, gbn_stats* stats) {
+  if (!h || !stats) return fail(h, GBN_ERR_INVALID_ARG, "gbn_get_stats: null argument");
+  *stats = h->stats;
+  return GBN_OK;
+}
+
+}  // extern "C"

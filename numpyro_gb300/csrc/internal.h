@@ -1,0 +1,59 @@
+// internal.h -- host-side declarations shared by the translation units of libgbnuts.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace gbn {
+
+struct AdvParams;
+
+// Device copy of a registry model plus the scratch its potential needs.
+struct ModelDev {
+  int family = 0;
+  int num_models = 1;
+  int64_t n = 0;
+  int p = 0;
+  int D = 0;               // latent dimension (max over models)
+  int chains_per_model = 1;
+  float* x = nullptr;      // [n][p]
+  float* y = nullptr;      // [n]
+  float* sigma = nullptr;  // [n]
+  int32_t* offsets = nullptr;
+  double hyper[8] = {0};
+  int precision = 0;
+  // scratch (sized for scratch_points potential points)
+  int scratch_points = 0;
+  int row_groups = 0;
+  float* part_g = nullptr;    // [row_groups][points][64]
+  double* part_ll = nullptr;  // [row_groups][points]
+  float* resid = nullptr;     // horseshoe [n][points]
+  float* part_gb = nullptr;   // horseshoe split-K partials
+  double* part_rr = nullptr;  // horseshoe [row tiles][points]
+  void* tc = nullptr;         // tensor-core path state (logreg_tc.cu)
+};
+
+// nuts_engine.cu
+void launch_advance(const AdvParams* dP, int C, int D, int parity, cudaStream_t st);
+void launch_init_uniform(const AdvParams* dP, int C, int D, int attempt, const int32_t* flag, cudaStream_t st);
+void launch_check_valid(const AdvParams* dP, int C, int32_t* flag, int32_t* count, cudaStream_t st);
+void launch_init_state(const AdvParams* dP, int C, int D, const float* inv_mass_init, float init_step,
+                       cudaStream_t st);
+void launch_set_phase(const AdvParams* dP, int C, int phase, int iters, cudaStream_t st);
+void launch_set_rng_chain(uint32_t* rng_key, int C, int first_chain, cudaStream_t st);
+
+// potentials_simt.cu: returns cudaError of the launch
+cudaError_t ensure_potential_scratch(ModelDev& m, int points);
+void free_potential_scratch(ModelDev& m);
+cudaError_t launch_potential(ModelDev& m, const float* Q, int npts, double* PE, float* G,
+                             const int32_t* pending, cudaStream_t st);
+// VJP: out[k] = cot[k] * grad U(z_k)
+cudaError_t launch_scale_rows(const double* cot, float* G, int npts, int D, cudaStream_t st);
+
+// logreg_tc.cu (tensor-core BF16 split-precision logistic potential)
+bool logreg_tc_supported(const ModelDev& m);
+cudaError_t logreg_tc_prepare(ModelDev& m, int points);
+void logreg_tc_free(ModelDev& m);
+cudaError_t logreg_tc_launch(ModelDev& m, const float* Q, int npts, double* PE, float* G, const int32_t* pending,
+                             cudaStream_t st);
+
+}  // namespace gbn

@@ -1,0 +1,736 @@
+// nuts_engine.cu -- the per-chain NUTS/HMC state machine ("advance" kernel).
+//
+// One group of threads (a warp, or a CTA for large D) owns one chain.  A
+// launch of advance_kernel consumes the gradient the potential kernel just
+// produced at the chain's query point, finishes that leapfrog step, runs the
+// tree logic, and stops at the next point where the chain needs a gradient
+// (its next leaf), writing that position into the query buffer Q.  The host
+// alternates advance / potential launches ("ticks").
+//
+// In the fused engine each chain doubles its own tree and starts its next
+// transition as soon as its tree ends, so every tick is a gradient for every
+// live chain.  In the plain engine (lockstep=1) a chain that finished its
+// transition waits until all chains have (numpyro's vmap'd while_loop
+// semantics, numpyro/infer/hmc.py:796-798), and the potential is evaluated
+// for every chain (masked lanes included).
+//
+// Reference arithmetic (numpyro/infer/hmc_util.py):
+//   velocity_verlet.update_fn :289-309, _build_basetree :851-894,
+//   _combine_tree :767-848 (uniform :749-753, biased :756-764),
+//   _iterative_build_subtree :984-1085, _leaf_idx_to_ckpt_idxs :941-958,
+//   _is_iterative_turning :961-981, _is_turning/_momentum_angle :710-746,
+//   build_tree :1088-1180, euclidean_kinetic_energy :1183-1223,
+//   dual_averaging :60-130, welford_covariance :133-239,
+//   warmup_adapter.update_fn :637-705, find_reasonable_step_size :314-384;
+// numpyro/infer/hmc.py: momentum_generator :92-110, _hmc_next :364-414,
+//   _nuts_next :416-455, sample_kernel :459-530.
+#include "common.cuh"
+#include "internal.h"
+
+namespace gbn {
+
+constexpr float FLT32_TINY = 1.17549435e-38f;
+constexpr float FLT32_MAX = 3.40282347e+38f;
+
+template <int NT>
+struct Chain {
+  const AdvParams& P;
+  Group<NT> g;
+  double* red;
+  int c;   // chain index
+  int D;   // this chain's latent dim
+  int ld;  // row stride of [C][ld] buffers
+  ChainCtl ctl;
+
+  __device__ __forceinline__ size_t row() const { return (size_t)c * ld; }
+  __device__ __forceinline__ float* V(float* base) const { return base + row(); }
+  __device__ __forceinline__ float* CK(float* base, int k) const { return base + ((size_t)c * P.maxd + k) * ld; }
+
+  // 0.5 * r . (M^-1 r)
+  __device__ double kinetic(const float* r) {
+    const float* mi = V(P.s.inverse_mass_matrix);
+    double acc = 0.0;
+    for (int d = g.tid; d < D; d += NT) acc += (double)mi[d] * (double)r[d] * (double)r[d];
+    return 0.5 * g.sum(acc, red);
+  }
+
+  // _is_turning: v_l . (rs - (r_l + r_r)/2) <= 0 or v_r . (...) <= 0, with v = M^-1 r
+  __device__ bool is_turning(const float* rl, const float* rr, const float* rs, const float* rs_minus,
+                             const float* rs_plus) {
+    const float* mi = V(P.s.inverse_mass_matrix);
+    double2 acc = make_double2(0.0, 0.0);
+    for (int d = g.tid; d < D; d += NT) {
+      double s = (double)rs[d];
+      if (rs_minus) s = s - (double)rs_minus[d] + (double)rs_plus[d];
+      double a = (double)rl[d], b = (double)rr[d];
+      s -= 0.5 * (a + b);
+      acc.x += (double)mi[d] * a * s;
+      acc.y += (double)mi[d] * b * s;
+    }
+    double2 t = g.sum2(acc, red);
+    return (t.x <= 0.0) || (t.y <= 0.0);
+  }
+
+  __device__ void copy(float* dst, const float* src) {
+    for (int d = g.tid; d < D; d += NT) dst[d] = src[d];
+  }
+
+  // ----------------------------------------------------------- leapfrog halves
+  // first half-kick + drift from the frontier on side `right`; writes Q
+  __device__ void leaf_prepare(bool right, float eps) {
+    float* z = V(right ? P.e.z_r : P.e.z_l);
+    float* r = V(right ? P.e.r_r : P.e.r_l);
+    const float* gr = V(right ? P.e.g_r : P.e.g_l);
+    const float* mi = V(P.s.inverse_mass_matrix);
+    float* q = V(P.e.Q);
+    for (int d = g.tid; d < D; d += NT) {
+      float rh = r[d] - 0.5f * eps * gr[d];
+      float zn = z[d] + eps * (mi[d] * rh);
+      r[d] = rh;
+      z[d] = zn;
+      q[d] = zn;
+    }
+  }
+  // second half-kick with the new gradient; returns K(r_new)
+  __device__ double leaf_finish(bool right, float eps) {
+    float* r = V(right ? P.e.r_r : P.e.r_l);
+    float* gr = V(right ? P.e.g_r : P.e.g_l);
+    const float* G = V(P.e.G);
+    for (int d = g.tid; d < D; d += NT) {
+      float gn = G[d];
+      r[d] = r[d] - 0.5f * eps * gn;
+      gr[d] = gn;
+    }
+    return kinetic(r);
+  }
+
+  __device__ float signed_step() const { return ctl.dir ? ctl.step : -ctl.step; }
+
+  // ----------------------------------------------------------- transitions
+  __device__ void start_transition() {
+    uint32_t n = P.s.rng_key[2 * c + 1];
+    uint32_t chain_id = P.s.rng_key[2 * c];
+    const float* ms = V(P.s.mass_matrix_sqrt);
+    const float* z = V(P.s.z);
+    const float* gz = V(P.s.z_grad);
+    float *zl = V(P.e.z_l), *zr = V(P.e.z_r), *zp = V(P.e.z_p);
+    float *rl = V(P.e.r_l), *rr = V(P.e.r_r), *rs = V(P.e.rsum);
+    float *gl = V(P.e.g_l), *grr = V(P.e.g_r), *gp = V(P.e.g_p);
+    double kin = 0.0;
+    const float* mi = V(P.s.inverse_mass_matrix);
+    for (int d = g.tid; d < D; d += NT) {
+      float r = ms[d] * normal_at(P.seed, chain_id, n, P_MOMENTUM, d, 0);
+      kin += (double)mi[d] * (double)r * (double)r;
+      float zz = z[d], gg = gz[d];
+      zl[d] = zz; zr[d] = zz; zp[d] = zz;
+      gl[d] = gg; grr[d] = gg; gp[d] = gg;
+      rl[d] = r; rr[d] = r; rs[d] = r;
+    }
+    kin = 0.5 * g.sum(kin, red);
+    int i = P.s.i[c];
+    double pe = P.s.potential_energy[c];
+    ctl.energy0 = pe + kin;
+    ctl.step = P.s.step_size[c];
+    ctl.depth = 0;
+    ctl.tree_w = 0.0;
+    ctl.tree_turning = 0;
+    ctl.tree_div = 0;
+    ctl.tree_acc = 0.0;
+    ctl.num_prop = 0;
+    ctl.pe_p = pe;
+    ctl.energy_p = ctl.energy0;
+    ctl.max_depth_cur = (i < P.num_warmup) ? P.mtd_warmup : P.mtd;
+    if (P.algo == 1) {  // fixed-length HMC, hmc.py:364-414
+      int L;
+      if (P.fixed_steps > 0) {
+        L = P.fixed_steps;
+      } else {
+        L = (int)ceil(P.traj_len / (double)ctl.step);
+      }
+      if (L < 1) L = 1;
+      if (P.traj_len > 0.0) ctl.step = (float)(P.traj_len / (double)L);
+      ctl.hmc_left = L;
+      ctl.hmc_total = L;
+      ctl.dir = 1;
+    }
+  }
+
+  __device__ void start_subtree() {
+    uint32_t n = P.s.rng_key[2 * c + 1];
+    uint32_t chain_id = P.s.rng_key[2 * c];
+    uint4 w = draw(P.seed, chain_id, n, P_DOUBLING, (uint32_t)ctl.depth, 0);
+    ctl.dir = u01d(w.x) < 0.5 ? 1 : 0;
+    ctl.sub_num = 0;
+    ctl.sub_div = 0;
+    ctl.sub_turning = 0;
+    leaf_prepare(ctl.dir, signed_step());
+    ctl.phase = PH_LEAF;
+  }
+
+  // a leaf's gradient has arrived: _build_basetree + uniform combine + checkpoints
+  __device__ void finish_leaf() {
+    uint32_t n = P.s.rng_key[2 * c + 1];
+    uint32_t chain_id = P.s.rng_key[2 * c];
+    bool right = ctl.dir;
+    double kin = leaf_finish(right, signed_step());
+    double pe = P.e.PE[c];
+    double e_new = pe + kin;
+    double dE = e_new - ctl.energy0;
+    if (isnan(dE)) dE = INFINITY;
+    double w = -dE;
+    int div = dE > P.max_dE;
+    double acc = fmin(exp(-dE), 1.0);
+    const float* zf = V(right ? P.e.z_r : P.e.z_l);
+    const float* rf = V(right ? P.e.r_r : P.e.r_l);
+    const float* gf = V(right ? P.e.g_r : P.e.g_l);
+    float* zsp = V(P.e.z_sp);
+    float* gsp = V(P.e.g_sp);
+    float* rss = V(P.e.rsum_sub);
+    int leaf_idx = ctl.sub_num;
+    if (leaf_idx == 0) {
+      for (int d = g.tid; d < D; d += NT) {
+        zsp[d] = zf[d];
+        gsp[d] = gf[d];
+        rss[d] = rf[d];
+      }
+      ctl.sub_w = w;
+      ctl.pe_sp = pe;
+      ctl.energy_sp = e_new;
+      ctl.sub_acc = acc;
+    } else {
+      double p = sigmoid_d(w - ctl.sub_w);
+      uint4 u = draw(P.seed, chain_id, n, P_LEAF, (uint32_t)ctl.depth, (uint32_t)leaf_idx);
+      bool take = u01d(u.x) < p;
+      for (int d = g.tid; d < D; d += NT) {
+        if (take) {
+          zsp[d] = zf[d];
+          gsp[d] = gf[d];
+        }
+        rss[d] += rf[d];
+      }
+      if (take) {
+        ctl.pe_sp = pe;
+        ctl.energy_sp = e_new;
+      }
+      ctl.sub_w = logaddexp_d(ctl.sub_w, w);
+      ctl.sub_acc += acc;
+    }
+    ctl.sub_div = div;
+    ctl.sub_num = leaf_idx + 1;
+    // checkpoints (hmc_util.py:1034-1047)
+    int idx_max = __popc((unsigned)(leaf_idx >> 1));
+    int num_sub = __popc((unsigned)((~leaf_idx & (leaf_idx + 1)) - 1));
+    int idx_min = idx_max - num_sub + 1;
+    if ((leaf_idx & 1) == 0) {
+      float* rck = CK(P.e.r_ck, idx_max);
+      float* sck = CK(P.e.rs_ck, idx_max);
+      for (int d = g.tid; d < D; d += NT) {
+        rck[d] = rf[d];
+        sck[d] = rss[d];
+      }
+    }
+    g.sync();
+    bool turning = false;
+    for (int k = idx_max; k >= idx_min && !turning; --k) {
+      // subtree r_sum = r_sum - r_sum_ckpts[k] + r_ckpts[k]; left = r_ckpts[k], right = r
+      turning = is_turning(CK(P.e.r_ck, k), rf, rss, CK(P.e.rs_ck, k), CK(P.e.r_ck, k));
+    }
+    ctl.sub_turning = turning;
+  }
+
+  // subtree done: biased combine into the tree (hmc_util.py:936-938 -> :767-848)
+  __device__ void combine_subtree() {
+    uint32_t n = P.s.rng_key[2 * c + 1];
+    uint32_t chain_id = P.s.rng_key[2 * c];
+    float* rs = V(P.e.rsum);
+    const float* rss = V(P.e.rsum_sub);
+    for (int d = g.tid; d < D; d += NT) rs[d] += rss[d];
+    g.sync();
+    double p;
+    if (ctl.sub_turning || ctl.sub_div) {
+      p = 0.0;
+    } else {
+      p = fmin(exp(ctl.sub_w - ctl.tree_w), 1.0);
+    }
+    bool turning = ctl.sub_turning;
+    if (!turning) turning = is_turning(V(P.e.r_l), V(P.e.r_r), rs, nullptr, nullptr);
+    uint4 u = draw(P.seed, chain_id, n, P_DOUBLING, (uint32_t)ctl.depth, 0);
+    bool take = u01d(u.y) < p;
+    if (take) {
+      copy(V(P.e.z_p), V(P.e.z_sp));
+      copy(V(P.e.g_p), V(P.e.g_sp));
+      ctl.pe_p = ctl.pe_sp;
+      ctl.energy_p = ctl.energy_sp;
+    }
+    ctl.depth += 1;
+    ctl.tree_w = logaddexp_d(ctl.tree_w, ctl.sub_w);
+    ctl.tree_div = ctl.sub_div;
+    ctl.tree_acc += ctl.sub_acc;
+    ctl.num_prop += ctl.sub_num;
+    ctl.tree_turning = turning;
+  }
+
+  // ----------------------------------------------------------- adaptation
+  // returns true if a heuristic step-size search was started (pending)
+  __device__ bool adapt(int t, double accept_prob) {
+    double* ss = P.s.ss_state + 5 * (size_t)c;
+    float step = P.s.step_size[c];
+    if (P.adapt_step) {  // dual_averaging.update_fn, t0=10, kappa=0.75, gamma=0.05
+      double g_ = (double)P.target_accept - accept_prob;
+      double x_t = ss[0], x_avg = ss[1], g_avg = ss[2], tt = ss[3], prox = ss[4];
+      tt += 1.0;
+      g_avg = (1.0 - 1.0 / (tt + 10.0)) * g_avg + g_ / (tt + 10.0);
+      x_t = prox - sqrt(tt) / 0.05 * g_avg;
+      double wt = pow(tt, -0.75);
+      x_avg = (1.0 - wt) * x_avg + wt * x_t;
+      ss[0] = x_t; ss[1] = x_avg; ss[2] = g_avg; ss[3] = tt;
+      double s = (t == P.num_warmup - 1) ? exp(x_avg) : exp(x_t);
+      float sf = (float)s;
+      if (!(sf >= FLT32_TINY)) sf = FLT32_TINY;  // also maps NaN to tiny
+      if (sf > FLT32_MAX) sf = FLT32_MAX;
+      step = sf;
+    }
+    int widx = P.s.window_idx[c];
+    bool middle = (0 < widx) && (widx < P.num_windows - 1);
+    const float* z = V(P.s.z);
+    double* mean = P.s.mm_mean + row();
+    double* m2 = P.s.mm_m2 + row();
+    if (P.adapt_mass && middle) {  // welford update_fn
+      int nn = P.s.mm_n[c] + 1;
+      for (int d = g.tid; d < D; d += NT) {
+        double x = (double)z[d];
+        double dpre = x - mean[d];
+        double mnew = mean[d] + dpre / nn;
+        mean[d] = mnew;
+        m2[d] += dpre * (x - mnew);
+      }
+      if (g.tid == 0) P.s.mm_n[c] = nn;
+    }
+    bool at_end = (t == P.window_end[widx]);
+    if (at_end) widx += 1;
+    if (g.tid == 0) P.s.window_idx[c] = widx;
+    bool started = false;
+    if (at_end && middle) {
+      if (P.adapt_mass) {  // welford final_fn + Stan regularisation
+        int nn = P.s.mm_n[c];
+        float* inv = V(P.s.inverse_mass_matrix);
+        float* sq = V(P.s.mass_matrix_sqrt);
+        float* sqi = V(P.s.mass_matrix_sqrt_inv);
+        for (int d = g.tid; d < D; d += NT) {
+          double cov = m2[d] / (double)(nn - 1);
+          if (P.regularize) cov = ((double)nn / (nn + 5.0)) * cov + 1e-3 * (5.0 / (nn + 5.0));
+          float covf = (float)cov;
+          float ti = sqrtf(covf);
+          inv[d] = covf;
+          sqi[d] = ti;
+          sq[d] = 1.0f / ti;
+          mean[d] = 0.0;
+          m2[d] = 0.0;
+        }
+        if (g.tid == 0) P.s.mm_n[c] = 0;
+      }
+      if (P.adapt_step) {
+        if (P.heuristic) {
+          if (g.tid == 0) P.s.step_size[c] = step;
+          g.sync();
+          heur_begin(HC_WINDOW, (uint32_t)t);
+          started = true;
+        } else {
+          ss[0] = 0.0; ss[1] = 0.0; ss[2] = 0.0; ss[3] = 0.0;
+          ss[4] = log(10.0) + log((double)step);
+        }
+      }
+    }
+    if (!started && g.tid == 0) P.s.step_size[c] = step;
+    g.sync();
+    return started;
+  }
+
+  // ----------------------------------------------------------- heuristic step size
+  // find_reasonable_step_size (hmc_util.py:314-384).  The trial momentum is
+  // generated from the inverse mass matrix, as the reference does at :356.
+  __device__ void heur_begin(int ctx, uint32_t n_ctx) {
+    ctl.heur_ctx = ctx;
+    ctl.heur_step = (double)P.s.step_size[c];
+    ctl.heur_dir = 0;
+    ctl.heur_last = 0;
+    ctl.heur_trial = 0;
+    ctl.hmc_total = (int)n_ctx;  // stream index of this search
+    heur_prepare();
+  }
+  __device__ void heur_prepare() {
+    uint32_t chain_id = P.s.rng_key[2 * c];
+    ctl.heur_step = exp2((double)ctl.heur_dir) * ctl.heur_step;
+    float eps = (float)ctl.heur_step;
+    const float* mi = V(P.s.inverse_mass_matrix);
+    const float* z = V(P.s.z);
+    const float* gz = V(P.s.z_grad);
+    float* r0 = V(P.e.r_l);
+    float* rh = V(P.e.r_r);
+    float* q = V(P.e.Q);
+    double kin = 0.0;
+    for (int d = g.tid; d < D; d += NT) {
+      float r = mi[d] * normal_at(P.seed, chain_id, (uint32_t)ctl.hmc_total, P_HEURISTIC, d,
+                                  (uint32_t)ctl.heur_trial);
+      kin += (double)mi[d] * (double)r * (double)r;
+      r0[d] = r;
+      float h = r - 0.5f * eps * gz[d];
+      rh[d] = h;
+      q[d] = z[d] + eps * (mi[d] * h);
+    }
+    ctl.heur_e0 = P.s.potential_energy[c] + 0.5 * g.sum(kin, red);
+    ctl.phase = PH_HEUR;
+  }
+  // returns true when the search is over (step size in ctl.heur_step)
+  __device__ bool heur_finish() {
+    float eps = (float)ctl.heur_step;
+    const float* mi = V(P.s.inverse_mass_matrix);
+    const float* G = V(P.e.G);
+    const float* rh = V(P.e.r_r);
+    double kin = 0.0;
+    for (int d = g.tid; d < D; d += NT) {
+      float rn = rh[d] - 0.5f * eps * G[d];
+      kin += (double)mi[d] * (double)rn * (double)rn;
+    }
+    double e_new = P.e.PE[c] + 0.5 * g.sum(kin, red);
+    double dE = e_new - ctl.heur_e0;
+    int dir_new = (log(0.8) < -dE) ? 1 : -1;
+    ctl.heur_last = ctl.heur_dir;
+    ctl.heur_dir = dir_new;
+    ctl.heur_trial += 1;
+    double s = ctl.heur_step;
+    bool not_small = (s > (double)FLT32_TINY) || (ctl.heur_dir >= 0);
+    bool not_large = (s < (double)FLT32_MAX) || (ctl.heur_dir <= 0);
+    bool cont = not_small && not_large && ((ctl.heur_last == 0) || (ctl.heur_dir == ctl.heur_last));
+    if (cont && ctl.heur_trial < 4096) {
+      heur_prepare();
+      return false;
+    }
+    return true;
+  }
+  __device__ void heur_done() {
+    float step = (float)ctl.heur_step;
+    double* ss = P.s.ss_state + 5 * (size_t)c;
+    if (g.tid == 0) {
+      P.s.step_size[c] = step;
+      ss[0] = 0.0; ss[1] = 0.0; ss[2] = 0.0; ss[3] = 0.0;
+      ss[4] = (ctl.heur_ctx == HC_INIT) ? log(10.0 * (double)step) : log(10.0) + log((double)step);
+    }
+    g.sync();
+  }
+
+  // ----------------------------------------------------------- end of transition
+  // returns true if the chain is now pending on a gradient (heuristic search)
+  __device__ bool finish_transition(double pe_new, double energy_new, int num_steps, double accept_prob,
+                                    int diverging, const float* znew, const float* gnew) {
+    float* z = V(P.s.z);
+    float* gz = V(P.s.z_grad);
+    if (znew != z) {
+      for (int d = g.tid; d < D; d += NT) {
+        z[d] = znew[d];
+        gz[d] = gnew[d];
+      }
+    }
+    g.sync();
+    int i = P.s.i[c];
+    int j = ctl.iters_done;
+    if (g.tid == 0) {
+      P.s.potential_energy[c] = pe_new;
+      P.s.energy[c] = energy_new;
+      P.s.num_steps[c] = num_steps;
+      P.s.accept_prob[c] = (float)accept_prob;
+      P.s.diverging[c] = (uint8_t)diverging;
+      int itr = i + 1;
+      int nn = (i < P.num_warmup) ? itr : itr - P.num_warmup;
+      float m = P.s.mean_accept_prob[c];
+      P.s.mean_accept_prob[c] = m + ((float)accept_prob - m) / (float)nn;
+      P.s.i[c] = itr;
+      P.s.rng_key[2 * c + 1] += 1u;
+    }
+    // collection
+    if (j >= P.collect_start && ((j - P.collect_start) % P.thinning) == 0) {
+      int sidx = (j - P.collect_start) / P.thinning;
+      if (sidx < P.num_collect) {
+        size_t o = (size_t)c * P.num_collect + sidx;
+        if (P.col.samples) {
+          float* dst = P.col.samples + o * ld;
+          for (int d = g.tid; d < D; d += NT) dst[d] = znew[d];
+        }
+        if (g.tid == 0) {
+          if (P.col.num_steps) P.col.num_steps[o] = num_steps;
+          if (P.col.accept_prob) P.col.accept_prob[o] = (float)accept_prob;
+          if (P.col.diverging) P.col.diverging[o] = (uint8_t)diverging;
+          if (P.col.potential_energy) P.col.potential_energy[o] = pe_new;
+        }
+      }
+    }
+    g.sync();
+    bool pending = false;
+    if (i < P.num_warmup) pending = adapt(i, accept_prob);
+    if (j >= P.collect_start && ((j - P.collect_start) % P.thinning) == 0 && !pending) {
+      int sidx = (j - P.collect_start) / P.thinning;
+      if (sidx < P.num_collect && P.col.step_size && g.tid == 0)
+        P.col.step_size[(size_t)c * P.num_collect + sidx] = P.s.step_size[c];
+    }
+    ctl.iters_done = j + 1;
+    ctl.iters_left -= 1;
+    if (P.lockstep && g.tid == 0) atomicAdd(&P.done_count[j], 1);
+    return pending;
+  }
+
+  // may a new transition start now?
+  __device__ bool may_start() {
+    if (ctl.iters_left <= 0) return false;
+    if (!P.lockstep || ctl.iters_done == 0) return true;
+    return *((volatile int32_t*)&P.done_count[ctl.iters_done - 1]) >= P.C;
+  }
+
+  // ----------------------------------------------------------- driver
+  __device__ void run() {
+    bool need_start = false;
+    switch (ctl.phase) {
+      case PH_START:
+        need_start = true;
+        break;
+      case PH_HEUR_START:
+        heur_begin(HC_INIT, INIT_TRANSITION);
+        return;
+      case PH_HEUR:
+        if (heur_finish()) {
+          heur_done();
+          if (ctl.heur_ctx == HC_INIT) {
+            ctl.phase = PH_DONE;
+            return;
+          }
+          need_start = true;  // window-end search finished: continue sampling
+        } else {
+          return;
+        }
+        break;
+      case PH_WAIT:
+        need_start = true;
+        break;
+      case PH_HMC: {
+        double kin = leaf_finish(true, ctl.step);
+        ctl.hmc_left -= 1;
+        if (ctl.hmc_left > 0) {
+          leaf_prepare(true, ctl.step);
+          return;
+        }
+        // Metropolis correction (hmc.py:395-414)
+        double pe = P.e.PE[c];
+        double e_new = pe + kin;
+        double dE = e_new - ctl.energy0;
+        if (isnan(dE)) dE = INFINITY;
+        double acc = fmin(exp(-dE), 1.0);
+        int div = dE > P.max_dE;
+        uint32_t n = P.s.rng_key[2 * c + 1];
+        uint32_t chain_id = P.s.rng_key[2 * c];
+        uint4 u = draw(P.seed, chain_id, n, P_HMC_ACCEPT, 0, 0);
+        bool take = u01d(u.x) < acc;
+        bool pend;
+        if (take)
+          pend = finish_transition(pe, e_new, ctl.hmc_total, acc, div, V(P.e.z_r), V(P.e.g_r));
+        else
+          pend = finish_transition(P.s.potential_energy[c], ctl.energy0, ctl.hmc_total, acc, div, V(P.s.z),
+                                   V(P.s.z_grad));
+        if (pend) return;
+        need_start = true;
+        break;
+      }
+      case PH_LEAF: {
+        finish_leaf();
+        bool cont_sub = (ctl.sub_num < (1 << ctl.depth)) && !ctl.sub_turning && !ctl.sub_div;
+        if (cont_sub) {
+          leaf_prepare(ctl.dir, signed_step());
+          return;
+        }
+        combine_subtree();
+        bool cont_tree = (ctl.depth < ctl.max_depth_cur) && !ctl.tree_turning && !ctl.tree_div;
+        if (cont_tree) {
+          start_subtree();
+          return;
+        }
+        double accept_prob = ctl.tree_acc / (double)ctl.num_prop;
+        bool pend = finish_transition(ctl.pe_p, ctl.energy_p, ctl.num_prop, accept_prob, ctl.tree_div,
+                                      V(P.e.z_p), V(P.e.g_p));
+        if (pend) return;
+        need_start = true;
+        break;
+      }
+      default:
+        return;
+    }
+    if (need_start) {
+      if (!may_start()) {
+        ctl.phase = (ctl.iters_left > 0) ? PH_WAIT : PH_DONE;
+        return;
+      }
+      start_transition();
+      if (P.algo == 1) {
+        leaf_prepare(true, ctl.step);
+        ctl.phase = PH_HMC;
+      } else {
+        start_subtree();  // depth 0 < max_depth always holds for max_tree_depth >= 1
+      }
+    }
+  }
+};
+
+template <int NT>
+__global__ void __launch_bounds__(256) advance_kernel(const AdvParams* __restrict__ Pp, int parity) {
+  __shared__ double red[16];
+  const AdvParams& P = *Pp;
+  int c;
+  int tid;
+  if (NT == 32) {
+    c = blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5);
+    tid = threadIdx.x & 31;
+  } else {
+    c = blockIdx.x;
+    tid = threadIdx.x;
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    P.counters[2 * (parity ^ 1)] = 0;
+    P.counters[2 * (parity ^ 1) + 1] = 0;
+  }
+  int pending = 0, active = 0;
+  if (c < P.C) {
+    Chain<NT> ch{P, Group<NT>{tid}, red, c, P.e.chain_dim ? P.e.chain_dim[c] : P.D, P.D, P.e.ctl[c]};
+    ch.run();
+    if (tid == 0) {
+      P.e.ctl[c] = ch.ctl;
+      int ph = ch.ctl.phase;
+      pending = (ph == PH_LEAF || ph == PH_HMC || ph == PH_HEUR);
+      active = (ph != PH_DONE && ph != PH_IDLE);
+    }
+  }
+  int np = __syncthreads_count(pending);
+  int na = __syncthreads_count(active);
+  if (threadIdx.x == 0) {
+    if (np) atomicAdd(&P.counters[2 * parity], np);
+    if (na) atomicAdd(&P.counters[2 * parity + 1], na);
+  }
+}
+
+// --------------------------------------------------------------------- init kernels
+// init_to_uniform(radius=2) for chains whose flag is set; writes z into st.z and Q
+__global__ void init_uniform_kernel(const AdvParams* __restrict__ Pp, int attempt, const int32_t* __restrict__ flag) {
+  const AdvParams& P = *Pp;
+  size_t total = (size_t)P.C * P.D;
+  for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < total; k += (size_t)gridDim.x * blockDim.x) {
+    int c = (int)(k / P.D), d = (int)(k % P.D);
+    if (flag && !flag[c]) continue;
+    int Dc = P.e.chain_dim ? P.e.chain_dim[c] : P.D;
+    float v = 0.0f;
+    if (d < Dc) v = -2.0f + 4.0f * uniform_at(P.seed, P.s.rng_key[2 * c], (uint32_t)attempt, P_INIT, d, 0);
+    P.s.z[k] = v;
+  }
+}
+
+// validity of (pe, grad) per chain: flag[c] = 1 when not finite; counts invalid
+__global__ void check_valid_kernel(const AdvParams* __restrict__ Pp, int32_t* flag, int32_t* count) {
+  const AdvParams& P = *Pp;
+  int c = blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5);
+  int lane = threadIdx.x & 31;
+  if (c >= P.C) return;
+  int Dc = P.e.chain_dim ? P.e.chain_dim[c] : P.D;
+  bool ok = true;
+  for (int d = lane; d < Dc; d += 32) ok &= isfinite(P.s.z_grad[(size_t)c * P.D + d]);
+  ok = __all_sync(0xffffffffu, ok);
+  ok = ok && isfinite(P.s.potential_energy[c]);
+  if (lane == 0) {
+    flag[c] = ok ? 0 : 1;
+    if (!ok) atomicAdd(count, 1);
+  }
+}
+
+// HMCState / HMCAdaptState initial values (hmc.py:193-362, hmc_util.py:552-594)
+__global__ void init_state_kernel(const AdvParams* __restrict__ Pp, const float* __restrict__ inv_mass_init,
+                                  float init_step) {
+  const AdvParams& P = *Pp;
+  size_t total = (size_t)P.C * P.D;
+  for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < total; k += (size_t)gridDim.x * blockDim.x) {
+    int c = (int)(k / P.D), d = (int)(k % P.D);
+    int Dc = P.e.chain_dim ? P.e.chain_dim[c] : P.D;
+    float inv = (d < Dc) ? (inv_mass_init ? inv_mass_init[k] : 1.0f) : 0.0f;
+    float si = sqrtf(inv);
+    P.s.inverse_mass_matrix[k] = inv;
+    P.s.mass_matrix_sqrt_inv[k] = si;
+    P.s.mass_matrix_sqrt[k] = (d < Dc) ? 1.0f / si : 0.0f;
+    P.s.mm_mean[k] = 0.0;
+    P.s.mm_m2[k] = 0.0;
+    if (d == 0) {
+      P.s.i[c] = 0;
+      P.s.num_steps[c] = 0;
+      P.s.accept_prob[c] = 0.0f;
+      P.s.mean_accept_prob[c] = 0.0f;
+      P.s.diverging[c] = 0;
+      P.s.step_size[c] = init_step;
+      double* ss = P.s.ss_state + 5 * (size_t)c;
+      ss[0] = 0.0; ss[1] = 0.0; ss[2] = 0.0; ss[3] = 0.0;
+      ss[4] = log(10.0 * (double)init_step);
+      P.s.mm_n[c] = 0;
+      P.s.window_idx[c] = 0;
+      P.s.rng_key[2 * c + 1] = 0u;
+      P.s.energy[c] = P.s.potential_energy[c];
+    }
+  }
+}
+
+__global__ void set_phase_kernel(const AdvParams* __restrict__ Pp, int phase, int iters) {
+  const AdvParams& P = *Pp;
+  int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= P.C) return;
+  ChainCtl& k = P.e.ctl[c];
+  k.phase = phase;
+  k.iters_left = iters;
+  k.iters_done = 0;
+}
+
+__global__ void set_rng_chain_kernel(uint32_t* rng_key, int C, int first_chain) {
+  int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c < C) {
+    rng_key[2 * c] = (uint32_t)(first_chain + c);
+    rng_key[2 * c + 1] = 0u;
+  }
+}
+
+// --------------------------------------------------------------------- launchers
+void launch_advance(const AdvParams* dP, int C, int D, int parity, cudaStream_t st) {
+  if (D <= 1024) {
+    int cpb = 8;
+    advance_kernel<32><<<(C + cpb - 1) / cpb, 32 * cpb, 0, st>>>(dP, parity);
+  } else {
+    advance_kernel<256><<<C, 256, 0, st>>>(dP, parity);
+  }
+}
+
+void launch_init_uniform(const AdvParams* dP, int C, int D, int attempt, const int32_t* flag, cudaStream_t st) {
+  size_t total = (size_t)C * D;
+  int blocks = (int)((total + 255) / 256);
+  if (blocks > 4096) blocks = 4096;
+  init_uniform_kernel<<<blocks, 256, 0, st>>>(dP, attempt, flag);
+}
+
+void launch_check_valid(const AdvParams* dP, int C, int32_t* flag, int32_t* count, cudaStream_t st) {
+  check_valid_kernel<<<(C + 7) / 8, 256, 0, st>>>(dP, flag, count);
+}
+
+void launch_init_state(const AdvParams* dP, int C, int D, const float* inv_mass_init, float init_step,
+                       cudaStream_t st) {
+  size_t total = (size_t)C * D;
+  int blocks = (int)((total + 255) / 256);
+  if (blocks > 4096) blocks = 4096;
+  init_state_kernel<<<blocks, 256, 0, st>>>(dP, inv_mass_init, init_step);
+}
+
+void launch_set_phase(const AdvParams* dP, int C, int phase, int iters, cudaStream_t st) {
+  set_phase_kernel<<<(C + 255) / 256, 256, 0, st>>>(dP, phase, iters);
+}
+
+void launch_set_rng_chain(uint32_t* rng_key, int C, int first_chain, cudaStream_t st) {
+  set_rng_chain_kernel<<<(C + 255) / 256, 256, 0, st>>>(rng_key, C, first_chain);
+}
+
+}  // namespace gbn

@@ -1,0 +1,107 @@
+"""MCMC driver on the GPU: API contract (numpyro/infer/mcmc.py) and posterior
+moments against the FP64 oracle (within 3 Monte-Carlo standard errors)."""
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+
+from numpyro_gb300 import MCMC, NUTS, HMC, datasets, diagnostics, models  # noqa: E402
+from oracle import nuts_ref as R  # noqa: E402
+from oracle import potentials_ref as PR  # noqa: E402
+
+
+def _mcse_ok(gpu, ref, k=3.0):
+    """|mean_gpu - mean_ref| within k * sqrt(mcse_gpu^2 + mcse_ref^2), per coordinate."""
+    m1, m2 = gpu.mean(axis=(0, 1)), ref.mean(axis=(0, 1))
+    s1, s2 = gpu.std(axis=(0, 1)), ref.std(axis=(0, 1))
+    e1 = np.array([diagnostics.effective_sample_size(gpu[..., d]) for d in range(gpu.shape[-1])])
+    e2 = np.array([diagnostics.effective_sample_size(ref[..., d]) for d in range(ref.shape[-1])])
+    mcse = np.sqrt(s1 ** 2 / e1 + s2 ** 2 / e2)
+    return np.abs(m1 - m2) <= k * mcse + 1e-6, m1, m2, mcse
+
+
+@pytest.mark.gpu
+def test_mcmc_api_eight_schools():
+    y, s = datasets.eight_schools(0)
+    model = models.HierarchicalNormal(y, s)
+    mcmc = MCMC(NUTS(model), num_warmup=300, num_samples=400, num_chains=4)
+    mcmc.run(0, extra_fields=("num_steps", "accept_prob", "adapt_state.step_size"))
+    samples = mcmc.get_samples()
+    assert samples["mu"].shape == (1600, 1) and samples["theta_base"].shape == (1600, 8)
+    assert np.all(samples["tau"] > 0)
+    grouped = mcmc.get_samples(group_by_chain=True)
+    assert grouped["mu"].shape == (4, 400, 1)
+    extra = mcmc.get_extra_fields()
+    assert extra["num_steps"].shape == (1600,) and extra["diverging"].shape == (1600,)
+    assert np.all(extra["num_steps"] >= 1)
+    assert 0.5 < extra["accept_prob"].mean() <= 1.0
+    assert np.all(np.diff(extra["adapt_state.step_size"].reshape(4, 400), axis=1) == 0)
+    mcmc.print_summary()
+    # warmup() then run() resumes from post_warmup_state without adapting
+    m2 = MCMC(NUTS(model), num_warmup=200, num_samples=100, num_chains=4)
+    m2.warmup(1)
+    st = m2.post_warmup_state
+    assert int(st.i[0]) == 200
+    m2.run(2)
+    assert m2.get_samples()["mu"].shape == (400, 1)
+    assert int(m2.last_state.i[0]) == 300
+
+
+@pytest.mark.gpu
+def test_eight_schools_posterior_matches_oracle():
+    y, s = datasets.eight_schools(0)
+    model = models.HierarchicalNormal(y, s)
+    C, W, S = 4, 500, 1000
+    mcmc = MCMC(NUTS(model), num_warmup=W, num_samples=S, num_chains=C)
+    mcmc.run(7, extra_fields=("z",))
+    zg = mcmc.get_extra_fields(group_by_chain=True)["z"]
+    pot = PR.make_potential("hier_nc", y.astype(np.float64), s.astype(np.float64))
+    ref = np.array([R.run_chain(pot, model.latent_dim, 99, c, W, S)[0] for c in range(C)])
+    ok, m1, m2, mcse = _mcse_ok(zg, ref)
+    assert ok.mean() >= 0.9, (m1, m2, mcse)
+    rhat = diagnostics.split_gelman_rubin(zg)
+    assert np.all(rhat < 1.05), rhat
+
+
+@pytest.mark.gpu
+def test_logistic_posterior_plain_and_fused():
+    X, yv, beta = datasets.covtype_like(seed=3, n=3000, n_cont=3, n_bin=3)
+    model = models.LogisticRegression(X, yv)
+    res = {}
+    for engine in ["fused", "plain"]:
+        mcmc = MCMC(NUTS(model, engine=engine), num_warmup=300, num_samples=500, num_chains=16)
+        mcmc.run(3)
+        res[engine] = mcmc.get_samples(group_by_chain=True)["coefs"]
+    np.testing.assert_array_equal(res["fused"], res["plain"])
+    pot = PR.make_potential("logreg", X.astype(np.float64), yv.astype(np.float64))
+    ref = np.array([R.run_chain(pot, X.shape[1], 5, c, 300, 500)[0] for c in range(4)])
+    ok, m1, m2, mcse = _mcse_ok(res["fused"], ref)
+    assert ok.mean() >= 0.85, (m1, m2, mcse)
+    assert np.all(diagnostics.split_gelman_rubin(res["fused"]) < 1.05)
+
+
+@pytest.mark.gpu
+def test_hmc_kernel_runs_and_adapts():
+    y, s = datasets.eight_schools(0)
+    model = models.HierarchicalNormal(y, s)
+    mcmc = MCMC(HMC(model, trajectory_length=1.5), num_warmup=200, num_samples=200, num_chains=8)
+    mcmc.run(4, extra_fields=("accept_prob",))
+    acc = mcmc.get_extra_fields()["accept_prob"]
+    assert 0.5 < acc.mean() <= 1.0
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["horseshoe", "sv"])
+def test_large_latent_families_run(name):
+    if name == "horseshoe":
+        X, yh, beta = datasets.horseshoe_data(seed=1, n=300, p=60, nonzero=4)
+        model = models.HorseshoeRegression(X, yh)
+    else:
+        r, _ = datasets.sv_returns(seed=1, T=600)
+        model = models.StochasticVolatility(r)
+    mcmc = MCMC(NUTS(model, max_tree_depth=8), num_warmup=150, num_samples=100, num_chains=8)
+    mcmc.run(1, extra_fields=("accept_prob",))
+    samp = mcmc.get_samples()
+    for v in samp.values():
+        assert np.all(np.isfinite(v))
+    assert mcmc.get_extra_fields()["accept_prob"].mean() > 0.3

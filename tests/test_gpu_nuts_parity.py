@@ -1,0 +1,174 @@
+"""NUTS/HMC transition parity: CUDA engine vs the FP64 oracle on identical Philox bits.
+
+Each GPU transition is replayed by the oracle from the GPU's own starting
+state (so FP32-vs-FP64 chaos cannot accumulate), with the same stream
+addresses.  Tree sizes (num_steps) must agree on >= 99.9% of transitions,
+positions within 1e-5 relative on trajectories that take the same decisions.
+"""
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+
+from numpyro_gb300 import HMC, NUTS, datasets, models  # noqa: E402
+from oracle import nuts_ref as R  # noqa: E402
+from oracle import philox  # noqa: E402
+from oracle import potentials_ref as PR  # noqa: E402
+
+SEED = 1234
+
+
+def _hier():
+    y, s = datasets.eight_schools(0)
+    return models.HierarchicalNormal(y, s), PR.make_potential("hier_nc", y.astype(np.float64), s.astype(np.float64))
+
+
+def _oracle_transition(pot, z, step, inv_mass, chain, n, algo="NUTS", max_tree_depth=10, traj=None, nsteps=None):
+    init_kernel, sample_kernel = R.hmc(pot, algo=algo)
+    kw = {}
+    if algo == "HMC":
+        kw = dict(trajectory_length=traj, num_steps=nsteps)
+    st = init_kernel(np.asarray(z, np.float64), 0, step_size=step, inverse_mass_matrix=np.asarray(inv_mass, np.float64),
+                     adapt_step_size=False, adapt_mass_matrix=False, max_tree_depth=max_tree_depth,
+                     rng_key=(SEED, chain), **kw)
+    st = st._replace(rng_key=R.RngKey(SEED, chain, n))
+    return sample_kernel(st)
+
+
+@pytest.mark.gpu
+def test_init_to_uniform_bits_match_oracle():
+    model, _ = _hier()
+    C = 64
+    k = NUTS(model, num_chains=C)
+    st = k.init(SEED, 0)
+    z = st.z.cpu().numpy()
+    for c in range(C):
+        np.testing.assert_array_equal(z[c], R.init_to_uniform(SEED, c, model.latent_dim).astype(np.float32))
+    k.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("engine", ["fused", "plain"])
+def test_single_transition_parity(engine):
+    model, pot = _hier()
+    C = 256
+    steps = [0.05, 0.2, 0.6, 1.5]
+    k = NUTS(model, num_chains=C, step_size=0.3, adapt_step_size=False, adapt_mass_matrix=False, engine=engine)
+    state = k.init(SEED, 0)
+    # per-chain step sizes and masses to exercise deep trees, U-turns and divergences
+    ss = torch.tensor([steps[c % 4] for c in range(C)], dtype=torch.float32, device="cuda")
+    inv = torch.as_tensor(np.random.default_rng(0).uniform(0.5, 2.0, (C, model.latent_dim)).astype(np.float32),
+                          device="cuda")
+    state.adapt_state.step_size.copy_(ss)
+    state.adapt_state.inverse_mass_matrix.copy_(inv)
+    state.adapt_state.mass_matrix_sqrt.copy_(1.0 / inv.sqrt())
+    same, total, zerr = 0, 0, []
+    for it in range(6):
+        z0 = state.z.cpu().numpy().copy()
+        new = k.sample(state)
+        zg = new.z.cpu().numpy()
+        ns = new.num_steps.cpu().numpy()
+        ap = new.accept_prob.cpu().numpy()
+        dv = new.diverging.cpu().numpy()
+        for c in range(C):
+            ref = _oracle_transition(pot, z0[c], steps[c % 4], inv[c].cpu().numpy(), c, it)
+            total += 1
+            if ref.num_steps == ns[c] and bool(ref.diverging) == bool(dv[c]):
+                same += 1
+                assert abs(ref.accept_prob - ap[c]) <= 1e-3 + 1e-3 * abs(ref.accept_prob)
+                zerr.append(np.max(np.abs(ref.z - zg[c]) / (np.abs(ref.z) + 1e-2)))
+        state = new
+    frac = same / total
+    assert frac >= 0.99, frac
+    assert np.median(zerr) < 1e-5, np.median(zerr)
+    k.close()
+
+
+@pytest.mark.gpu
+def test_fused_and_plain_engines_are_bit_identical():
+    model, _ = _hier()
+    res = {}
+    for engine in ["fused", "plain"]:
+        k = NUTS(model, num_chains=32, engine=engine)
+        st = k.init(SEED, 100)
+        out = k.run_device(st, 150, collect_start=0, collect=("z", "num_steps"))
+        res[engine] = (out["z"].cpu().numpy(), out["num_steps"].cpu().numpy(), st.adapt_state.step_size.cpu().numpy())
+        k.close()
+    for a, b in zip(res["fused"], res["plain"]):
+        np.testing.assert_array_equal(a, b)
+
+
+@pytest.mark.gpu
+def test_warmup_adaptation_tracks_oracle():
+    """First iterations of warmup (dual averaging) follow the oracle's step-size sequence."""
+    model, pot = _hier()
+    C = 8
+    k = NUTS(model, num_chains=C)
+    st = k.init(SEED, 50)
+    gpu_steps = []
+    for it in range(8):
+        st = k.sample(st)
+        gpu_steps.append(st.adapt_state.step_size.cpu().numpy().copy())
+    gpu_steps = np.array(gpu_steps)
+    agree = 0
+    for c in range(C):
+        init_kernel, sample_kernel = R.hmc(pot)
+        ost = init_kernel(R.init_to_uniform(SEED, c, model.latent_dim), 50, rng_key=(SEED, c))
+        seq = []
+        for it in range(8):
+            ost = sample_kernel(ost)
+            seq.append(ost.adapt_state.step_size)
+        if np.allclose(np.array(seq), gpu_steps[:, c], rtol=1e-4):
+            agree += 1
+    assert agree >= C - 1, agree
+    k.close()
+
+
+@pytest.mark.gpu
+def test_hmc_fixed_steps_parity():
+    model, pot = _hier()
+    C = 64
+    k = HMC(model, num_chains=C, step_size=0.1, num_steps=7, trajectory_length=None, adapt_step_size=False,
+            adapt_mass_matrix=False)
+    st = k.init(SEED, 0)
+    z0 = st.z.cpu().numpy()
+    new = k.sample(st)
+    zg = new.z.cpu().numpy()
+    ap = new.accept_prob.cpu().numpy()
+    for c in range(C):
+        ref = _oracle_transition(pot, z0[c], 0.1, np.ones(model.latent_dim), c, 0, algo="HMC", traj=None, nsteps=7)
+        assert new.num_steps.cpu().numpy()[c] == 7
+        assert abs(ref.accept_prob - ap[c]) < 1e-4
+        np.testing.assert_allclose(zg[c], ref.z, rtol=1e-5, atol=1e-5)
+    k.close()
+
+
+@pytest.mark.gpu
+def test_divergence_large_step():
+    """test/infer/test_hmc_util.py:406-442 invariant: huge steps diverge in one leaf."""
+    model, _ = _hier()
+    k = NUTS(model, num_chains=16, step_size=100.0, adapt_step_size=False)
+    st = k.sample(k.init(SEED, 0))
+    assert bool(st.diverging.all())
+    assert int(st.num_steps.max()) == 1
+    k.close()
+
+
+@pytest.mark.gpu
+def test_uneven_batched_models_match_single_model_runs():
+    """One launch over models of different J gives each model the result of running it alone."""
+    ds = datasets.uneven_hierarchical(seed=0, num_models=6, jmin=3, jmax=20)
+    batched = models.HierarchicalNormal(datasets=ds)
+    kb = NUTS(batched, num_chains=12)
+    sb = kb.init(SEED, 30)
+    outb = kb.run_device(sb, 40, collect_start=30, collect=("z",))["z"].cpu().numpy()
+    kb.close()
+    # model 2 alone with the same chain ids (4, 5) -> same stream addresses
+    m2 = models.HierarchicalNormal(*ds[2])
+    k2 = NUTS(m2, num_chains=6)
+    s2 = k2.init(SEED, 30)
+    out2 = k2.run_device(s2, 40, collect_start=30, collect=("z",))["z"].cpu().numpy()
+    k2.close()
+    D2 = m2.latent_dim
+    np.testing.assert_array_equal(outb[4:6, :, :D2], out2[4:6])
+    assert np.all(outb[4:6, :, D2:] == 0)
