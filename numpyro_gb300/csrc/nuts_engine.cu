@@ -306,7 +306,7 @@ struct Chain {
       }
       if (g.tid == 0) P.s.mm_n[c] = nn;
     }
-    bool at_end = (t == P.window_end[widx]);
+    bool at_end = (widx < P.num_windows) && (t == P.window_end[widx]);
     if (at_end) widx += 1;
     if (g.tid == 0) P.s.window_idx[c] = widx;
     bool started = false;

@@ -25,7 +25,8 @@ constexpr double LOG_2 = 0.6931471805599453;
 // z = [mu, log tau, theta_base(J)];  warp per point; model m = point / cpm
 __global__ void __launch_bounds__(256) hier_nc_kernel(const float* __restrict__ Q, int npts, int ld,
                                                       const float* __restrict__ y, const float* __restrict__ sg,
-                                                      const int32_t* __restrict__ off, int cpm, double mu_scale,
+                                                      const int32_t* __restrict__ off, int cpm, int num_models,
+                                                      double mu_scale,
                                                       double tau_scale, double* __restrict__ PE,
                                                       float* __restrict__ G, const int32_t* pending) {
   if (pending && *pending == 0) return;
@@ -33,6 +34,7 @@ __global__ void __launch_bounds__(256) hier_nc_kernel(const float* __restrict__ 
   int lane = threadIdx.x & 31;
   if (c >= npts) return;
   int m = c / cpm;
+  if (m >= num_models) m = num_models - 1;  // points beyond the configured chains reuse the last model
   int j0 = off[m], J = off[m + 1] - j0;
   const float* z = Q + (size_t)c * ld;
   float* g = G + (size_t)c * ld;
@@ -452,7 +454,7 @@ cudaError_t launch_potential(ModelDev& m, const float* Q, int npts, double* PE, 
   switch (m.family) {
     case 1:
       hier_nc_kernel<<<(npts + 7) / 8, 256, 0, st>>>(Q, npts, ld, m.y, m.sigma, m.offsets, m.chains_per_model,
-                                                      m.hyper[0], m.hyper[1], PE, G, pending);
+                                                      m.num_models, m.hyper[0], m.hyper[1], PE, G, pending);
       break;
     case 2: {
       if (m.precision == 1 && m.tc) return logreg_tc_launch(m, Q, npts, PE, G, pending, st);

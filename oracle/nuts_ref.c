@@ -1,0 +1,422 @@
+/*
+ * nuts_ref.c -- C restatement of numpyro's NUTS transition and warmup
+ * (ORACLE / CPU BASELINE: test infrastructure, never linked into the product).
+ *
+ * Follows numpyro/infer/hmc_util.py: velocity_verlet :262-311,
+ * _build_basetree :851-894, _combine_tree :767-848, _iterative_build_subtree
+ * :984-1085, _leaf_idx_to_ckpt_idxs :941-958, _is_iterative_turning
+ * :961-981, build_tree :1088-1180, dual_averaging :60-130,
+ * welford_covariance :133-239, build_adaptation_schedule :387-436,
+ * warmup_adapter :518-707; numpyro/infer/hmc.py sample_kernel :459-530.
+ * Randomness: Philox4x32-10 at the stream addresses of oracle/philox.py.
+ *
+ * Build: REAL=double (FP64 oracle) or REAL=float (FP32, numpyro's default
+ * dtype; sums accumulate in double).  OpenMP runs independent chains in
+ * parallel (the CPU analogue of chain_method="parallel").
+ */
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+#include <time.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#ifndef REAL
+#define REAL double
+#endif
+typedef REAL real;
+
+/* ------------------------------------------------------------------ Philox */
+static void philox(const uint32_t ctr[4], uint32_t k0, uint32_t k1, uint32_t out[4]) {
+  uint32_t c0 = ctr[0], c1 = ctr[1], c2 = ctr[2], c3 = ctr[3];
+  for (int r = 0; r < 10; ++r) {
+    uint64_t p0 = (uint64_t)0xD2511F53u * c0, p1 = (uint64_t)0xCD9E8D57u * c2;
+    uint32_t hi0 = (uint32_t)(p0 >> 32), lo0 = (uint32_t)p0, hi1 = (uint32_t)(p1 >> 32), lo1 = (uint32_t)p1;
+    c0 = hi1 ^ c1 ^ k0;
+    c1 = lo1;
+    c2 = hi0 ^ c3 ^ k1;
+    c3 = lo0;
+    k0 += 0x9E3779B9u;
+    k1 += 0xBB67AE85u;
+  }
+  out[0] = c0; out[1] = c1; out[2] = c2; out[3] = c3;
+}
+
+typedef struct { uint32_t lo, hi; } seed_t;
+enum { P_MOMENTUM = 0, P_DOUBLING = 1, P_LEAF = 2, P_INIT = 3 };
+
+static void draw(seed_t s, uint32_t chain, uint32_t n, uint32_t purpose, uint32_t idx, uint32_t sub, uint32_t o[4]) {
+  uint32_t c[4] = {chain, n, (purpose << 24) | idx, sub};
+  philox(c, s.lo, s.hi, o);
+}
+static double u01(uint32_t w) { return (double)(w >> 8) * (1.0 / 16777216.0); }
+
+static void normals(seed_t s, uint32_t chain, uint32_t n, uint32_t purpose, int dim, real* out) {
+  for (int k = 0; 4 * k < dim; ++k) {
+    uint32_t w[4];
+    draw(s, chain, n, purpose, (uint32_t)k, 0, w);
+    for (int pr = 0; pr < 2; ++pr) {
+      double u0 = u01(w[2 * pr]), u1 = u01(w[2 * pr + 1]);
+      double rad = sqrt(-2.0 * log1p(-u0)), ang = 2.0 * M_PI * u1;
+      int d0 = 4 * k + 2 * pr;
+      if (d0 < dim) out[d0] = (real)(rad * cos(ang));
+      if (d0 + 1 < dim) out[d0 + 1] = (real)(rad * sin(ang));
+    }
+  }
+}
+
+/* ------------------------------------------------------------------ potentials */
+typedef struct {
+  int family; /* 1 hier_nc, 2 logreg */
+  int64_t N;
+  int D;
+  const float* X;
+  const float* y;
+  const float* sigma;
+  double hyper[4];
+} model_t;
+
+/* numpyro potential_energy of the logistic model (examples/covtype.py:66-71):
+ * one fused pass over the rows; per-row arithmetic in `real`, sums in double. */
+static double logreg_pg(const model_t* m, const real* b, real* g) {
+  int D = m->D;
+  double ll = 0.0;
+  double* ga = (double*)calloc((size_t)D, sizeof(double));
+  for (int64_t n = 0; n < m->N; ++n) {
+    const float* x = m->X + n * D;
+    real l = 0;
+    for (int d = 0; d < D; ++d) l += (real)x[d] * b[d];
+    real t = (real)exp(-fabs((double)l));
+    real sp = (l > 0 ? l : (real)0) + (real)log1p((double)t);
+    real sig = l >= 0 ? (real)1 / ((real)1 + t) : t / ((real)1 + t);
+    real yy = (real)m->y[n];
+    ll += (double)(sp - yy * l);
+    real e = sig - yy;
+    for (int d = 0; d < D; ++d) ga[d] += (double)(e * (real)x[d]);
+  }
+  double pr = 0.0, s = m->hyper[0] > 0 ? m->hyper[0] : 1.0;
+  for (int d = 0; d < D; ++d) {
+    g[d] = (real)(ga[d] + (double)b[d] / (s * s));
+    pr += 0.5 * (double)b[d] * (double)b[d] / (s * s) + 0.5 * log(2 * M_PI) + log(s);
+  }
+  free(ga);
+  return ll + pr;
+}
+
+/* non-centred hierarchical normal, z = [mu, log tau, theta_base(J)] */
+static double hier_pg(const model_t* m, const real* z, real* g) {
+  int J = (int)m->N;
+  double ms = m->hyper[0] > 0 ? m->hyper[0] : 5.0, ts = m->hyper[1] > 0 ? m->hyper[1] : 5.0;
+  double mu = z[0], lt = z[1], tau = exp(lt);
+  double lp = -0.5 * (mu / ms) * (mu / ms) - 0.5 * log(2 * M_PI) - log(ms);
+  lp += -log(M_PI) - log(ts) - log1p((tau / ts) * (tau / ts)) + log(2.0) + lt;
+  double sw = 0, swe = 0;
+  for (int j = 0; j < J; ++j) {
+    double eta = z[2 + j], s = m->sigma[j], th = mu + tau * eta, r = (m->y[j] - th) / s;
+    lp += -0.5 * eta * eta - 0.5 * r * r - log(s) - log(2 * M_PI);
+    double w = r / s;
+    sw += w;
+    swe += w * eta;
+    g[2 + j] = (real)(eta - tau * w);
+  }
+  g[0] = (real)(mu / (ms * ms) - sw);
+  g[1] = (real)(2 * tau * tau / (ts * ts + tau * tau) - 1 - tau * swe);
+  return -lp;
+}
+
+static double potential_grad(const model_t* m, const real* z, real* g) {
+  return m->family == 2 ? logreg_pg(m, z, g) : hier_pg(m, z, g);
+}
+
+/* ------------------------------------------------------------------ chain */
+typedef struct {
+  int D, maxd;
+  real *z, *g, *inv, *msq;
+  real *zl, *rl, *gl, *zr, *rr, *gr, *zp, *gp, *zsp, *gsp, *rs, *rss, *rck, *sck, *tmp;
+  double pe, step, ss[5];
+  double *mean, *m2;
+  int mm_n, window_idx;
+  long grad_evals;
+} chain_t;
+
+static double kinetic(const chain_t* c, const real* r) {
+  double k = 0;
+  for (int d = 0; d < c->D; ++d) k += (double)c->inv[d] * (double)r[d] * (double)r[d];
+  return 0.5 * k;
+}
+
+static int is_turning(const chain_t* c, const real* rl, const real* rr, const real* rs, const real* rsm,
+                      const real* rsp) {
+  double a = 0, b = 0;
+  for (int d = 0; d < c->D; ++d) {
+    double s = rs[d];
+    if (rsm) s = s - rsm[d] + rsp[d];
+    s -= 0.5 * ((double)rl[d] + (double)rr[d]);
+    a += (double)c->inv[d] * rl[d] * s;
+    b += (double)c->inv[d] * rr[d] * s;
+  }
+  return a <= 0 || b <= 0;
+}
+
+static double logaddexp(double a, double b) {
+  double mx = a > b ? a : b;
+  if (mx == -INFINITY) return -INFINITY;
+  return mx + log1p(exp(-fabs(a - b)));
+}
+
+/* one leapfrog from the frontier (z, r, g) in place; returns pe */
+static double leapfrog(const model_t* m, chain_t* c, real* z, real* r, real* g, double eps) {
+  for (int d = 0; d < c->D; ++d) {
+    r[d] = (real)((double)r[d] - 0.5 * eps * g[d]);
+    z[d] = (real)((double)z[d] + eps * (double)c->inv[d] * r[d]);
+  }
+  double pe = potential_grad(m, z, g);
+  c->grad_evals++;
+  for (int d = 0; d < c->D; ++d) r[d] = (real)((double)r[d] - 0.5 * eps * g[d]);
+  return pe;
+}
+
+/* One NUTS transition (hmc.py:459-530 with build_tree hmc_util.py:1088-1180). */
+static void nuts_transition(const model_t* m, chain_t* c, seed_t s, uint32_t chain, uint32_t n, int max_depth,
+                            int* num_steps, double* accept_prob, int* diverging) {
+  int D = c->D;
+  real* r0 = c->tmp;
+  normals(s, chain, n, P_MOMENTUM, D, r0);
+  for (int d = 0; d < D; ++d) r0[d] *= c->msq[d];
+  double e0 = c->pe + kinetic(c, r0);
+  memcpy(c->zl, c->z, D * sizeof(real)); memcpy(c->zr, c->z, D * sizeof(real)); memcpy(c->zp, c->z, D * sizeof(real));
+  memcpy(c->gl, c->g, D * sizeof(real)); memcpy(c->gr, c->g, D * sizeof(real)); memcpy(c->gp, c->g, D * sizeof(real));
+  memcpy(c->rl, r0, D * sizeof(real)); memcpy(c->rr, r0, D * sizeof(real)); memcpy(c->rs, r0, D * sizeof(real));
+  int depth = 0, turning = 0, div = 0, nprop = 0;
+  double tw = 0, tacc = 0, pe_p = c->pe;
+  while (depth < max_depth && !turning && !div) {
+    uint32_t w[4];
+    draw(s, chain, n, P_DOUBLING, (uint32_t)depth, 0, w);
+    int right = u01(w[0]) < 0.5;
+    double eps = right ? c->step : -c->step;
+    real *zf = right ? c->zr : c->zl, *rf = right ? c->rr : c->rl, *gf = right ? c->gr : c->gl;
+    int snum = 0, sdiv = 0, sturn = 0, maxn = 1 << depth;
+    double sw = 0, sacc = 0, pe_sp = 0;
+    while (snum < maxn && !sturn && !sdiv) {
+      double pe = leapfrog(m, c, zf, rf, gf, eps);
+      double dE = pe + kinetic(c, rf) - e0;
+      if (isnan(dE)) dE = INFINITY;
+      double lw = -dE, acc = exp(-dE) < 1 ? exp(-dE) : 1.0;
+      int leaf = snum;
+      if (leaf == 0) {
+        memcpy(c->zsp, zf, D * sizeof(real)); memcpy(c->gsp, gf, D * sizeof(real)); memcpy(c->rss, rf, D * sizeof(real));
+        sw = lw; pe_sp = pe; sacc = acc;
+      } else {
+        uint32_t u[4];
+        draw(s, chain, n, P_LEAF, (uint32_t)depth, (uint32_t)leaf, u);
+        double p = 1.0 / (1.0 + exp(-(lw - sw)));
+        if (u01(u[0]) < p) {
+          memcpy(c->zsp, zf, D * sizeof(real)); memcpy(c->gsp, gf, D * sizeof(real));
+          pe_sp = pe;
+        }
+        for (int d = 0; d < D; ++d) c->rss[d] += rf[d];
+        sw = logaddexp(sw, lw);
+        sacc += acc;
+      }
+      sdiv = dE > 1000.0;
+      snum++;
+      int idx_max = __builtin_popcount((unsigned)(leaf >> 1));
+      int nsub = __builtin_popcount((unsigned)((~leaf & (leaf + 1)) - 1));
+      int idx_min = idx_max - nsub + 1;
+      if ((leaf & 1) == 0) {
+        memcpy(c->rck + (size_t)idx_max * D, rf, D * sizeof(real));
+        memcpy(c->sck + (size_t)idx_max * D, c->rss, D * sizeof(real));
+      }
+      for (int k = idx_max; k >= idx_min && !sturn; --k)
+        sturn = is_turning(c, c->rck + (size_t)k * D, rf, c->rss, c->sck + (size_t)k * D, c->rck + (size_t)k * D);
+    }
+    for (int d = 0; d < D; ++d) c->rs[d] += c->rss[d];
+    double p = (sturn || sdiv) ? 0.0 : (exp(sw - tw) < 1 ? exp(sw - tw) : 1.0);
+    turning = sturn || is_turning(c, c->rl, c->rr, c->rs, NULL, NULL);
+    if (u01(w[1]) < p) {
+      memcpy(c->zp, c->zsp, D * sizeof(real)); memcpy(c->gp, c->gsp, D * sizeof(real));
+      pe_p = pe_sp;
+    }
+    depth++;
+    tw = logaddexp(tw, sw);
+    div = sdiv;
+    tacc += sacc;
+    nprop += snum;
+  }
+  memcpy(c->z, c->zp, D * sizeof(real));
+  memcpy(c->g, c->gp, D * sizeof(real));
+  c->pe = pe_p;
+  *num_steps = nprop;
+  *accept_prob = tacc / nprop;
+  *diverging = div;
+}
+
+static int window_ends(int num_steps, int* ends) {
+  int k = 0;
+  if (num_steps <= 0) return 0;
+  if (num_steps < 20) { ends[k++] = num_steps - 1; return k; }
+  int sb = 75, eb = 50, iw = 25;
+  if (sb + eb + iw > num_steps) { sb = (int)(0.15 * num_steps); eb = (int)(0.1 * num_steps); iw = num_steps - sb - eb; }
+  ends[k++] = sb - 1;
+  int ews = num_steps - eb, ns = iw, nst = sb;
+  while (nst < ews) {
+    int cs = nst, cz = ns;
+    if (3 * cz <= ews - cs) ns = 2 * cz; else cz = ews - cs;
+    nst = cs + cz;
+    ends[k++] = nst - 1;
+  }
+  ends[k++] = num_steps - 1;
+  return k;
+}
+
+/* warmup_adapter.update_fn (hmc_util.py:637-705), diagonal mass, no heuristic */
+static void adapt(chain_t* c, int t, double accept_prob, int num_warmup, const int* ends, int nwin) {
+  double* ss = c->ss;
+  ss[3] += 1.0;
+  double tt = ss[3];
+  ss[2] = (1 - 1 / (tt + 10)) * ss[2] + (0.8 - accept_prob) / (tt + 10);
+  ss[0] = ss[4] - pow(tt, 0.5) / 0.05 * ss[2];
+  double wt = pow(tt, -0.75);
+  ss[1] = (1 - wt) * ss[1] + wt * ss[0];
+  double st = (t == num_warmup - 1) ? exp(ss[1]) : exp(ss[0]);
+  real sf = (real)st; /* step size carried in the build's precision */
+  if (!(sf >= (real)1.17549435e-38)) sf = (real)1.17549435e-38;
+  c->step = sf;
+  int mid = (0 < c->window_idx) && (c->window_idx < nwin - 1);
+  if (mid) {
+    c->mm_n++;
+    for (int d = 0; d < c->D; ++d) {
+      double x = c->z[d], dp = x - c->mean[d];
+      c->mean[d] += dp / c->mm_n;
+      c->m2[d] += dp * (x - c->mean[d]);
+    }
+  }
+  int at_end = c->window_idx < nwin && t == ends[c->window_idx];
+  if (at_end) c->window_idx++;
+  if (at_end && mid) {
+    int nn = c->mm_n;
+    for (int d = 0; d < c->D; ++d) {
+      double cov = c->m2[d] / (nn - 1);
+      cov = ((double)nn / (nn + 5.0)) * cov + 1e-3 * (5.0 / (nn + 5.0));
+      c->inv[d] = (real)cov;
+      c->msq[d] = (real)(1.0 / sqrt((double)(real)cov));
+      c->mean[d] = 0; c->m2[d] = 0;
+    }
+    c->mm_n = 0;
+    ss[0] = ss[1] = ss[2] = ss[3] = 0;
+    ss[4] = log(10.0) + log(c->step);
+  }
+}
+
+static double now_s(void) {
+  struct timespec ts;
+  clock_gettime(CLOCK_MONOTONIC, &ts);
+  return ts.tv_sec + 1e-9 * ts.tv_nsec;
+}
+
+/*
+ * Runs `chains` independent chains (ids first_chain..) for num_warmup +
+ * num_samples NUTS transitions.  If init_z is given ([chains][D], with
+ * init_step/init_inv), warmup adaptation is skipped and num_warmup
+ * transitions run without adaptation.  samples: [chains][num_samples][D].
+ * timing: [warmup_s, sampling_s, warmup_grad_evals, sampling_grad_evals, threads].
+ */
+int nutsref_run(int family, const float* X, const float* y, const float* sigma, int64_t N, int D, double h0,
+                double h1, int chains, int first_chain, int num_warmup, int num_samples, uint64_t seed,
+                int max_tree_depth, int threads, const float* init_z, const float* init_step,
+                const float* init_inv, float* samples, int32_t* num_steps_out, double* timing) {
+  model_t m = {family, N, D, X, y, sigma, {h0, h1, 0, 0}};
+  seed_t s = {(uint32_t)(seed & 0xffffffffu), (uint32_t)(seed >> 32)};
+  int ends[64];
+  int nwin = window_ends(num_warmup, ends);
+  double tw0 = 0, tw1 = 0, ts1 = 0;
+  long gw = 0, gs = 0;
+#ifdef _OPENMP
+  if (threads > 0) omp_set_num_threads(threads);
+#endif
+  chain_t* cs = (chain_t*)calloc((size_t)chains, sizeof(chain_t));
+  int maxd = max_tree_depth;
+  for (int k = 0; k < chains; ++k) {
+    chain_t* c = &cs[k];
+    c->D = D;
+    c->maxd = maxd;
+    real** vs[] = {&c->z, &c->g, &c->inv, &c->msq, &c->zl, &c->rl, &c->gl, &c->zr, &c->rr, &c->gr, &c->zp,
+                   &c->gp, &c->zsp, &c->gsp, &c->rs, &c->rss, &c->tmp};
+    for (size_t v = 0; v < sizeof(vs) / sizeof(vs[0]); ++v) *vs[v] = (real*)calloc((size_t)D, sizeof(real));
+    c->rck = (real*)calloc((size_t)maxd * D, sizeof(real));
+    c->sck = (real*)calloc((size_t)maxd * D, sizeof(real));
+    c->mean = (double*)calloc((size_t)D, sizeof(double));
+    c->m2 = (double*)calloc((size_t)D, sizeof(double));
+    uint32_t chain = (uint32_t)(first_chain + k);
+    if (init_z) {
+      for (int d = 0; d < D; ++d) {
+        c->z[d] = init_z[(size_t)k * D + d];
+        c->inv[d] = init_inv[(size_t)k * D + d];
+        c->msq[d] = (real)(1.0 / sqrt((double)c->inv[d]));
+      }
+      c->step = init_step[k];
+    } else {
+      for (int b = 0; 4 * b < D; ++b) {
+        uint32_t w[4];
+        draw(s, chain, 0, P_INIT, (uint32_t)b, 0, w);
+        for (int j = 0; j < 4 && 4 * b + j < D; ++j) c->z[4 * b + j] = (real)(-2.0 + 4.0 * u01(w[j]));
+      }
+      for (int d = 0; d < D; ++d) { c->inv[d] = 1; c->msq[d] = 1; }
+      c->step = 1.0;
+    }
+    c->ss[4] = log(10.0 * c->step);
+  }
+  tw0 = now_s();
+#pragma omp parallel for schedule(dynamic, 1) reduction(+ : gw)
+  for (int k = 0; k < chains; ++k) {
+    chain_t* c = &cs[k];
+    c->pe = potential_grad(&m, c->z, c->g);
+    uint32_t chain = (uint32_t)(first_chain + k);
+    for (int t = 0; t < num_warmup; ++t) {
+      int ns, dv;
+      double ap;
+      nuts_transition(&m, c, s, chain, (uint32_t)t, max_tree_depth, &ns, &ap, &dv);
+      if (!init_z) adapt(c, t, ap, num_warmup, ends, nwin);
+    }
+    gw += c->grad_evals;
+    c->grad_evals = 0;
+  }
+  tw1 = now_s();
+#pragma omp parallel for schedule(dynamic, 1) reduction(+ : gs)
+  for (int k = 0; k < chains; ++k) {
+    chain_t* c = &cs[k];
+    uint32_t chain = (uint32_t)(first_chain + k);
+    for (int t = 0; t < num_samples; ++t) {
+      int ns, dv;
+      double ap;
+      nuts_transition(&m, c, s, chain, (uint32_t)(num_warmup + t), max_tree_depth, &ns, &ap, &dv);
+      for (int d = 0; d < D; ++d) samples[((size_t)k * num_samples + t) * D + d] = (float)c->z[d];
+      if (num_steps_out) num_steps_out[(size_t)k * num_samples + t] = ns;
+    }
+    gs += c->grad_evals;
+  }
+  ts1 = now_s();
+  int nthreads = 1;
+#ifdef _OPENMP
+  nthreads = omp_get_max_threads();
+#endif
+  timing[0] = tw1 - tw0;
+  timing[1] = ts1 - tw1;
+  timing[2] = (double)gw;
+  timing[3] = (double)gs;
+  timing[4] = (double)nthreads;
+  if (init_z == NULL && init_step) {
+    /* return the adapted state through the init pointers' shapes is not supported */
+  }
+  for (int k = 0; k < chains; ++k) {
+    chain_t* c = &cs[k];
+    real** vs[] = {&c->z, &c->g, &c->inv, &c->msq, &c->zl, &c->rl, &c->gl, &c->zr, &c->rr, &c->gr, &c->zp,
+                   &c->gp, &c->zsp, &c->gsp, &c->rs, &c->rss, &c->tmp};
+    for (size_t v = 0; v < sizeof(vs) / sizeof(vs[0]); ++v) free(*vs[v]);
+    free(c->rck); free(c->sck); free(c->mean); free(c->m2);
+  }
+  free(cs);
+  return 0;
+}

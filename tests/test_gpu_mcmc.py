@@ -53,8 +53,9 @@ def test_eight_schools_posterior_matches_oracle():
     model = models.HierarchicalNormal(y, s)
     C, W, S = 4, 500, 1000
     mcmc = MCMC(NUTS(model), num_warmup=W, num_samples=S, num_chains=C)
-    mcmc.run(7, extra_fields=("z",))
-    zg = mcmc.get_extra_fields(group_by_chain=True)["z"]
+    mcmc.run(7)
+    g = mcmc.get_samples(group_by_chain=True)
+    zg = np.concatenate([g["mu"], np.log(g["tau"]), g["theta_base"]], axis=-1)  # unconstrained layout
     pot = PR.make_potential("hier_nc", y.astype(np.float64), s.astype(np.float64))
     ref = np.array([R.run_chain(pot, model.latent_dim, 99, c, W, S)[0] for c in range(C)])
     ok, m1, m2, mcse = _mcse_ok(zg, ref)
