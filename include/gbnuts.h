@@ -141,6 +141,8 @@ typedef struct {
 } gbn_stats;
 
 int gbn_abi_version(void);
+/* 1 when this GPU runs the tcgen05 (sm_103a) tensor-core potentials, else 0 */
+int gbn_tc_available(void);
 const char* gbn_last_error(gbn_handle h); /* h may be NULL: last global error */
 
 int gbn_create(gbn_handle* out, const gbn_model_desc* model, const gbn_config* cfg);

@@ -118,6 +118,7 @@ class Stats(ctypes.Structure):
 
 EXPORTS = {
     "gbn_abi_version": (ctypes.c_int, []),
+    "gbn_tc_available": (ctypes.c_int, []),
     "gbn_last_error": (ctypes.c_char_p, [ctypes.c_void_p]),
     "gbn_create": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(ModelDesc), ctypes.POINTER(Config)]),
     "gbn_destroy": (ctypes.c_int, [ctypes.c_void_p]),

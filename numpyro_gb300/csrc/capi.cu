@@ -129,6 +129,14 @@ extern "C" {
 
 int gbn_abi_version(void) { return GBN_ABI_VERSION; }
 
+int gbn_tc_available(void) {
+  ModelDev probe;
+  probe.family = GBN_FAMILY_LOGREG;
+  probe.p = 1;
+  probe.n = 1;
+  return logreg_tc_supported(probe) ? 1 : 0;
+}
+
 const char* gbn_last_error(gbn_handle h) { return h ? h->err.c_str() : g_last_error.c_str(); }
 
 int gbn_latent_dim(gbn_handle h, int32_t* dim) {
@@ -284,6 +292,11 @@ int gbn_create(gbn_handle* out, const gbn_model_desc* md, const gbn_config* cfg)
       return fail(nullptr, GBN_ERR_UNSUPPORTED, "bf16x3 tensor-core logistic path unavailable for this shape");
     }
     ce = logreg_tc_prepare(m, C);
+    if (ce == cudaErrorNotSupported) {
+      gbn_destroy(h);
+      return fail(nullptr, GBN_ERR_UNSUPPORTED,
+                  "bf16x3 needs a design matrix exactly representable in bfloat16 (use precision fp32)");
+    }
   }
   if (ce == cudaSuccess) ce = ensure_potential_scratch(m, C);
   if (ce != cudaSuccess) {
@@ -366,6 +379,8 @@ static int tick_loop(gbn_handle h, cudaStream_t st, int64_t max_ticks) {
     cudaError_t e = cudaMemcpyAsync(h->h_counters, h->counters, sizeof(int32_t) * 4, cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return cuda_fail(h, e, "tick loop");
+    if (h->m.tc && logreg_tc_error(h->m))
+      return fail(h, GBN_ERR_TIMEOUT, "tensor-core potential: a device wait timed out");
     if (h->h_counters[2 * last + 1] == 0) break;
     if (ticks > max_ticks) return fail(h, GBN_ERR_TIMEOUT, "tick budget exhausted: chains did not finish");
   }

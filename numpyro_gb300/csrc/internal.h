@@ -53,6 +53,7 @@ cudaError_t launch_scale_rows(const double* cot, float* G, int npts, int D, cuda
 bool logreg_tc_supported(const ModelDev& m);
 cudaError_t logreg_tc_prepare(ModelDev& m, int points);
 void logreg_tc_free(ModelDev& m);
+int logreg_tc_error(const ModelDev& m);  // nonzero: a device wait timed out
 cudaError_t logreg_tc_launch(ModelDev& m, const float* Q, int npts, double* PE, float* G, const int32_t* pending,
                              cudaStream_t st);
 

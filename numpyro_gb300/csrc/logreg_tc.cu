@@ -1,14 +1,584 @@
-// logreg_tc.cu -- tensor-core (tcgen05) BF16 split-precision logistic potential.
+// logreg_tc.cu -- tensor-core (tcgen05 + TMA + TMEM) logistic-regression potential.
+//
+// U(b) = sum_n [softplus(l_n) - y_n l_n] + sum_d b_d^2 / (2 s^2) + const,  l = X b
+// dU/db = X^T (sigmoid(l) - y) + b / s^2
+// (numpyro: BernoulliLogits.log_prob discrete.py:263 via
+//  binary_cross_entropy_with_logits distributions/util.py:317-320, Normal prior
+//  continuous.py:2975-2989, potential_energy infer/util.py:333-358.)
+//
+// One CTA owns 128 chains and a strided set of 128-row tiles of X:
+//   warp 0      TMA producer: X tile [128 rows x 64 feat] bf16, 128B swizzle, 4-stage ring
+//   warp 1      MMA issuer:  GEMM1  L[128 rows x 128 chains] = X_tile . (b_hi + b_mid + b_lo)^T
+//                            (three K=64 BF16 products accumulate in FP32 in TMEM, so the
+//                            FP32 coefficients are represented exactly: "bf16x3"),
+//                            GEMM2  G[128 chains x 64 feat] += E^T . X_tile  (E = sigmoid(L) - y)
+//   warps 2..9  epilogue: tcgen05.ld of L, sigmoid/softplus, compensated FP32 sums of the
+//               log-likelihood (warp transposed reductions), E as bf16 into shared memory.
+// L is double-buffered in TMEM (2 x 128 columns) so GEMM1 of tile t+1 overlaps the
+// epilogue of tile t; G lives in TMEM for the whole launch (64 columns).
+// The design matrix must be exactly representable in bf16 (checked on the host).
+// Every mbarrier wait is bounded; on a timeout the CTA records an error, drains its
+// in-flight copies and MMAs (bounded), frees TMEM and returns.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+#include <cuda_bf16.h>
+
+#include <cstdio>
+#include <vector>
+
 #include "common.cuh"
 #include "internal.h"
 
 namespace gbn {
+namespace tc {
 
-bool logreg_tc_supported(const ModelDev&) { return false; }
-cudaError_t logreg_tc_prepare(ModelDev&, int) { return cudaErrorNotSupported; }
-void logreg_tc_free(ModelDev&) {}
-cudaError_t logreg_tc_launch(ModelDev&, const float*, int, double*, float*, const int32_t*, cudaStream_t) {
-  return cudaErrorNotSupported;
+constexpr int BM = 128;  // rows per tile
+constexpr int BN = 128;  // chains per CTA
+constexpr int BK = 64;   // padded features: one 128-byte swizzle row of bf16
+constexpr int NSPLIT = 3;
+constexpr int STAGES = 4;
+constexpr int X_TILE = BM * BK * 2;  // 16 KB
+constexpr int B_TILE = BN * BK * 2;  // 16 KB
+constexpr int S_TILE = BM * BN * 2;  // 32 KB
+constexpr int OFF_X = 0;
+constexpr int OFF_B = OFF_X + STAGES * X_TILE;
+constexpr int OFF_S = OFF_B + NSPLIT * B_TILE;
+constexpr int OFF_MISC = OFF_S + 2 * S_TILE;
+constexpr int NUM_BARS = 2 * STAGES + 2 + 2 + 2 + 2 + 1;
+constexpr int SMEM_BYTES = OFF_MISC + 256 + BN * 8 + 1024;  // + alignment slack
+constexpr int NUM_THREADS = 320;
+constexpr uint32_t TMEM_COLS = 512;
+constexpr uint32_t ACC2_COL = 256;
+constexpr uint32_t WAIT_LIMIT = 1u << 22;
+
+enum { B_XFULL = 0, B_XEMPTY = STAGES, B_ACCF = 2 * STAGES, B_ACCE = 2 * STAGES + 2, B_SF = 2 * STAGES + 4,
+       B_SE = 2 * STAGES + 6, B_DONE = 2 * STAGES + 8 };
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void bar_init(uint32_t a, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(a), "r"(count) : "memory");
+}
+__device__ __forceinline__ void bar_arrive(uint32_t a) {
+  asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.shared::cta.b64 st, [%0];\n\t}" ::"r"(a) : "memory");
+}
+__device__ __forceinline__ void bar_expect_tx(uint32_t a, uint32_t bytes) {
+  asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n\t}" ::"r"(a),
+               "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ bool bar_try(uint32_t a, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(a), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// bounded wait: false on timeout or when another role already aborted
+__device__ __forceinline__ bool bar_wait(uint32_t a, uint32_t parity, volatile int* abort_flag, int* err) {
+  for (uint32_t i = 0; i < WAIT_LIMIT; ++i) {
+    if (bar_try(a, parity)) return true;
+    if (*abort_flag) return false;
+  }
+  *abort_flag = 1;
+  atomicExch(err, 4);
+  return false;
+}
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map, int x, int y, uint32_t bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+          dst),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(bar)
+      : "memory");
+}
+
+// shared-memory matrix descriptor (tcgen05): start>>4 [0,14), LBO>>4 [16,30), SBO>>4 [32,46),
+// fixed 0b001 at [46,49), base offset 0, swizzle mode at [61,64) (2 = 128-byte swizzle)
+__device__ __forceinline__ uint64_t sdesc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+  return (uint64_t)((addr >> 4) & 0x3FFFu) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
+         ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46) | (2ull << 61);
+}
+// instruction descriptor, kind::f16: D=f32 (bit 4), A=B=bf16 (bits 7, 10), A/B major at 15/16,
+// N>>3 at [17,23), M>>4 at [24,29)
+__host__ __device__ constexpr uint32_t idesc(int M, int N, int a_mn_major, int b_mn_major) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)a_mn_major << 15) | ((uint32_t)b_mn_major << 16) |
+         ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+__device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t id, uint32_t acc) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem_d),
+      "l"(a), "l"(b), "r"(id), "r"(acc)
+      : "memory");
+}
+__device__ __forceinline__ void mma_commit(uint32_t bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
+}
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+#pragma unroll
+  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+__device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+__device__ __forceinline__ float ex2_approx(float x) {
+  float y;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+__device__ __forceinline__ float lg2_approx(float x) {
+  float y;
+  asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+__device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
+  __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+  return *reinterpret_cast<uint32_t*>(&h);
+}
+
+struct Params {
+  const float* y;
+  int64_t n;
+  const __nv_bfloat16* bsplit;  // [chain_blocks*128][3][64]
+  int npts;
+  int row_groups;
+  float* part_g;    // [row_groups][npts][64]
+  double* part_ll;  // [row_groups][npts]
+  int* err;
+  const int32_t* pending;
+};
+
+__global__ void __launch_bounds__(NUM_THREADS, 1) logreg_tc_kernel(const __grid_constant__ CUtensorMap tmap_x,
+                                                                   Params P) {
+  if (P.pending && *P.pending == 0) return;
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + OFF_MISC);
+  uint32_t* tmem_holder = reinterpret_cast<uint32_t*>(smem + OFF_MISC + NUM_BARS * 8);
+  volatile int* abort_flag = reinterpret_cast<volatile int*>(smem + OFF_MISC + NUM_BARS * 8 + 4);
+  double* ll_smem = reinterpret_cast<double*>(smem + OFF_MISC + 256);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int cb = blockIdx.x;  // chain block
+  const int rg = blockIdx.y;  // row group
+  const int64_t ntiles = (P.n + BM - 1) / BM;
+  const int my_tiles = (int)((ntiles - rg + P.row_groups - 1) / P.row_groups);
+  auto bar = [&](int i) { return smem_u32(&bars[i]); };
+
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < STAGES; ++i) {
+      bar_init(bar(B_XFULL + i), 1);
+      bar_init(bar(B_XEMPTY + i), 1);
+    }
+    for (int i = 0; i < 2; ++i) {
+      bar_init(bar(B_ACCF + i), 1);
+      bar_init(bar(B_ACCE + i), 8);
+      bar_init(bar(B_SF + i), 8);
+      bar_init(bar(B_SE + i), 1);
+    }
+    bar_init(bar(B_DONE), 1);
+    *abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  for (int i = threadIdx.x; i < BN; i += NUM_THREADS) ll_smem[i] = 0.0;
+  // coefficient splits -> K-major 128B-swizzled tiles [128 chains][64 feat] (one per split)
+  {
+    const uint4* src = reinterpret_cast<const uint4*>(P.bsplit + (size_t)cb * BN * NSPLIT * BK);
+    for (int i = threadIdx.x; i < BN * NSPLIT * (BK / 8); i += NUM_THREADS) {
+      int chunk = i % (BK / 8);
+      int k = (i / (BK / 8)) % NSPLIT;
+      int c = i / (NSPLIT * (BK / 8));
+      uint4 v = src[i];
+      uint32_t off = OFF_B + k * B_TILE + (c >> 3) * 1024 + (c & 7) * 128 + ((chunk ^ (c & 7)) << 4);
+      *reinterpret_cast<uint4*>(smem + off) = v;
+    }
+  }
+  fence_proxy_async();
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_holder)),
+                 "r"(TMEM_COLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tmem_holder;
+
+  if (warp == 0) {
+    // ------------------------------------------------------------ TMA producer
+    if (lane == 0) {
+      int issued = 0;
+      for (int i = 0; i < my_tiles; ++i) {
+        int s = i % STAGES;
+        if (i >= STAGES && !bar_wait(bar(B_XEMPTY + s), ((i / STAGES) - 1) & 1, abort_flag, P.err)) break;
+        int64_t row0 = ((int64_t)rg + (int64_t)i * P.row_groups) * BM;
+        bar_expect_tx(bar(B_XFULL + s), X_TILE);
+        tma_load_2d(smem_u32(smem + OFF_X + s * X_TILE), &tmap_x, 0, (int)row0, bar(B_XFULL + s));
+        issued = i + 1;
+      }
+      if (*abort_flag) {  // drain copies still in flight before the CTA can exit
+        for (int i = (issued > STAGES ? issued - STAGES : 0); i < issued; ++i) {
+          int s = i % STAGES;
+          for (uint32_t k = 0; k < WAIT_LIMIT && !bar_try(bar(B_XFULL + s), (i / STAGES) & 1); ++k) {
+          }
+        }
+      }
+    }
+  } else if (warp == 1) {
+    // ------------------------------------------------------------ MMA issuer
+    if (lane == 0) {
+      constexpr uint32_t ID1 = idesc(BM, BN, 0, 0);  // L = X . B^T, both K-major
+      constexpr uint32_t ID2 = idesc(BN, BK, 1, 1);  // G = E^T . X, both MN-major
+      const uint32_t xb = smem_u32(smem + OFF_X), bb = smem_u32(smem + OFF_B), sb = smem_u32(smem + OFF_S);
+      bool ok = true;
+      int committed_gemm2 = -1;
+      for (int i = 0; i <= my_tiles && ok; ++i) {
+        if (i < my_tiles) {
+          int s = i % STAGES, b = i & 1;
+          ok = bar_wait(bar(B_XFULL + s), (i / STAGES) & 1, abort_flag, P.err);
+          if (ok && i >= 2) ok = bar_wait(bar(B_ACCE + b), ((i >> 1) - 1) & 1, abort_flag, P.err);
+          if (!ok) break;
+          tc_fence_after();
+          const uint32_t d = tmem + (uint32_t)(b * BN);
+          int first = 1;
+#pragma unroll
+          for (int k = 0; k < NSPLIT; ++k) {
+#pragma unroll
+            for (int kk = 0; kk < BK / 16; ++kk) {
+              uint64_t a = sdesc(xb + s * X_TILE + kk * 32, 16, 1024);
+              uint64_t bd = sdesc(bb + k * B_TILE + kk * 32, 16, 1024);
+              mma_bf16(d, a, bd, ID1, first ? 0u : 1u);
+              first = 0;
+            }
+          }
+          mma_commit(bar(B_ACCF + b));
+        }
+        if (i >= 1) {
+          int j = i - 1, s = j % STAGES, b = j & 1;
+          ok = bar_wait(bar(B_SF + b), (j >> 1) & 1, abort_flag, P.err);
+          if (!ok) break;
+          tc_fence_after();
+#pragma unroll
+          for (int kk = 0; kk < BM / 16; ++kk) {
+            // A = E[b]: MN-major, 64-chain atoms 1024 B apart (LBO), 8-row groups 2048 B apart (SBO)
+            uint64_t a = sdesc(sb + b * S_TILE + kk * 4096, 1024, 2048);
+            // B = X tile: MN-major (features contiguous), 8-row groups 1024 B apart (SBO)
+            uint64_t bd = sdesc(xb + s * X_TILE + kk * 2048, 1024, 1024);
+            mma_bf16(tmem + ACC2_COL, a, bd, ID2, (j > 0 || kk > 0) ? 1u : 0u);
+          }
+          mma_commit(bar(B_SE + b));
+          mma_commit(bar(B_XEMPTY + s));
+          committed_gemm2 = j;
+        }
+      }
+      mma_commit(bar(B_DONE));
+      (void)committed_gemm2;
+      // wait for every MMA issued by this thread before TMEM can be released
+      for (uint32_t k = 0; k < WAIT_LIMIT && !bar_try(bar(B_DONE), 0); ++k) {
+      }
+    }
+  } else {
+    // ------------------------------------------------------------ epilogue (warps 2..9)
+    const int ew = warp - 2;
+    const int q = warp & 3;         // TMEM lane quadrant this warp may access
+    const int ch = ew >> 2;         // column half: chains [64*ch, 64*ch+64)
+    const int row = q * 32 + lane;  // row within the tile
+    float kah_s[4] = {0.f, 0.f, 0.f, 0.f}, kah_c[4] = {0.f, 0.f, 0.f, 0.f};
+    const float LOG2E = 1.4426950408889634f, LN2 = 0.6931471805599453f;
+    bool ok = true;
+    for (int i = 0; i < my_tiles && ok; ++i) {
+      const int b = i & 1;
+      const int64_t grow = ((int64_t)rg + (int64_t)i * P.row_groups) * BM + row;
+      const bool valid = grow < P.n;
+      const float yv = valid ? P.y[grow] : 0.0f;
+      ok = bar_wait(bar(B_ACCF + b), (i >> 1) & 1, abort_flag, P.err);
+      if (ok && i >= 2) ok = bar_wait(bar(B_SE + b), ((i >> 1) - 1) & 1, abort_flag, P.err);
+      if (!ok) break;
+      tc_fence_after();
+      uint8_t* sdst = smem + OFF_S + b * S_TILE + (row >> 3) * 2048 + (row & 7) * 128;
+#pragma unroll 1
+      for (int j = 0; j < 4; ++j) {
+        const int col = ch * 64 + j * 16;
+        float v[16];
+        tmem_ld16(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(b * BN + col), v);
+        tmem_wait_ld();
+        if (j == 3) {
+          tc_fence_before();
+          __syncwarp();
+          if (lane == 0) bar_arrive(bar(B_ACCE + b));
+        }
+        float ll[16];
+        uint32_t pk[8];
+#pragma unroll
+        for (int e = 0; e < 16; e += 2) {
+          float ev[2];
+#pragma unroll
+          for (int h = 0; h < 2; ++h) {
+            const float l = v[e + h];
+            const float t = ex2_approx(-fabsf(l) * LOG2E);  // exp(-|l|)
+            const float u = 1.0f + t;
+            const float lg = lg2_approx(u);                // log2(1 + exp(-|l|))
+            // 1/u by Newton-Raphson from the linear estimate 24/17 - 8/17 u on [1, 2]
+            float r = fmaf(-0.47058823529411764f, u, 1.4117647058823530f);
+            float er = fmaf(-u, r, 1.0f);
+            r = fmaf(r, er, r);
+            er = fmaf(-u, r, 1.0f);
+            r = fmaf(r, er, r);
+            const float sig = (l >= 0.0f) ? r : t * r;
+            const float sp = fmaxf(l, 0.0f) + lg * LN2;
+            ll[e + h] = valid ? fmaf(-yv, l, sp) : 0.0f;
+            ev[h] = valid ? (sig - yv) : 0.0f;
+          }
+          pk[e >> 1] = pack_bf16(ev[0], ev[1]);
+        }
+        // E[row][col..col+15] -> two 16-byte chunks of the swizzled MN-major tile
+#pragma unroll
+        for (int hh = 0; hh < 2; ++hh) {
+          const int c8 = (col >> 3) + hh;  // 8-chain chunk index in [0,16)
+          const int atom = c8 >> 3, chunk = c8 & 7;
+          uint4 w = make_uint4(pk[4 * hh], pk[4 * hh + 1], pk[4 * hh + 2], pk[4 * hh + 3]);
+          *reinterpret_cast<uint4*>(sdst + atom * 1024 + ((chunk ^ (row & 7)) << 4)) = w;
+        }
+        // transposed butterfly: lane l ends with the 32-row sum of chain col + (l >> 1)
+#pragma unroll
+        for (int i8 = 0; i8 < 8; ++i8) {
+          const bool up = lane & 16;
+          float mine = up ? ll[8 + i8] : ll[i8];
+          float give = up ? ll[i8] : ll[8 + i8];
+          ll[i8] = mine + __shfl_xor_sync(0xffffffffu, give, 16);
+        }
+#pragma unroll
+        for (int i4 = 0; i4 < 4; ++i4) {
+          const bool up = lane & 8;
+          float mine = up ? ll[4 + i4] : ll[i4];
+          float give = up ? ll[i4] : ll[4 + i4];
+          ll[i4] = mine + __shfl_xor_sync(0xffffffffu, give, 8);
+        }
+#pragma unroll
+        for (int i2 = 0; i2 < 2; ++i2) {
+          const bool up = lane & 4;
+          float mine = up ? ll[2 + i2] : ll[i2];
+          float give = up ? ll[i2] : ll[2 + i2];
+          ll[i2] = mine + __shfl_xor_sync(0xffffffffu, give, 4);
+        }
+        {
+          const bool up = lane & 2;
+          float mine = up ? ll[1] : ll[0];
+          float give = up ? ll[0] : ll[1];
+          ll[0] = mine + __shfl_xor_sync(0xffffffffu, give, 2);
+        }
+        ll[0] += __shfl_xor_sync(0xffffffffu, ll[0], 1);
+        // compensated (Kahan) accumulation across tiles
+        {
+          float yk = ll[0] - kah_c[j];
+          float tk = kah_s[j] + yk;
+          kah_c[j] = (tk - kah_s[j]) - yk;
+          kah_s[j] = tk;
+        }
+      }
+      fence_proxy_async();
+      __syncwarp();
+      if (lane == 0) bar_arrive(bar(B_SF + b));
+    }
+    // per-chain log-likelihood of this CTA's rows
+    if (ok && (lane & 1) == 0) {
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const int c = ch * 64 + j * 16 + (lane >> 1);
+        atomicAdd(&ll_smem[c], (double)kah_s[j] - (double)kah_c[j]);
+      }
+    }
+    // gradient partials: G (lanes = chains, 64 feature columns)
+    if (ok) ok = bar_wait(bar(B_DONE), 0, abort_flag, P.err);
+    if (ok) {
+      tc_fence_after();
+      const int c = q * 32 + lane;
+      const int gc = cb * BN + c;
+#pragma unroll
+      for (int j = 0; j < 2; ++j) {
+        float v[16];
+        const int colb = ch * 32 + j * 16;
+        tmem_ld16(tmem + ((uint32_t)(q * 32) << 16) + ACC2_COL + (uint32_t)colb, v);
+        tmem_wait_ld();
+        if (gc < P.npts) {
+          float4* dst = reinterpret_cast<float4*>(P.part_g + ((size_t)rg * P.npts + gc) * 64 + colb);
+#pragma unroll
+          for (int k = 0; k < 4; ++k) dst[k] = make_float4(v[4 * k], v[4 * k + 1], v[4 * k + 2], v[4 * k + 3]);
+        }
+      }
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (!*abort_flag) {
+    for (int i = threadIdx.x; i < BN; i += NUM_THREADS) {
+      const int gc = cb * BN + i;
+      if (gc < P.npts) P.part_ll[(size_t)rg * P.npts + gc] = ll_smem[i];
+    }
+  }
+  if (warp == 1) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS) : "memory");
+  }
+}
+
+// b (fp32, [npts][ld]) -> [blocks*128][3][64] bf16 with b = hi + mid + lo exactly
+__global__ void split_coefs_kernel(const float* __restrict__ Q, int npts, int ld, int p, int npad,
+                                   __nv_bfloat16* __restrict__ out, const int32_t* pending) {
+  if (pending && *pending == 0) return;
+  int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= npad * BK) return;
+  int c = idx / BK, d = idx % BK;
+  float v = (c < npts && d < p) ? Q[(size_t)c * ld + d] : 0.0f;
+  __nv_bfloat16 hi = __float2bfloat16_rn(v);
+  float r1 = v - __bfloat162float(hi);
+  __nv_bfloat16 mid = __float2bfloat16_rn(r1);
+  float r2 = r1 - __bfloat162float(mid);
+  __nv_bfloat16 lo = __float2bfloat16_rn(r2);
+  __nv_bfloat16* o = out + ((size_t)c * NSPLIT) * BK + d;
+  o[0] = hi;
+  o[BK] = mid;
+  o[2 * BK] = lo;
+}
+
+__global__ void to_bf16_kernel(const float* __restrict__ x, int64_t n, int p, __nv_bfloat16* __restrict__ out,
+                               int* inexact) {
+  int64_t total = n * BK;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
+    int64_t r = i / BK;
+    int d = (int)(i % BK);
+    float v = (d < p) ? x[r * p + d] : 0.0f;
+    __nv_bfloat16 h = __float2bfloat16_rn(v);
+    if (__bfloat162float(h) != v) atomicExch(inexact, 1);
+    out[i] = h;
+  }
+}
+
+struct TCState {
+  __nv_bfloat16* xb = nullptr;
+  __nv_bfloat16* bsplit = nullptr;
+  CUtensorMap tmap;
+  int* err = nullptr;
+  int bsplit_pts = 0;
+  int row_groups = 0;
+  int chain_blocks = 0;
+  bool ok = false;
+};
+
+}  // namespace tc
+
+static PFN_cuTensorMapEncodeTiled_v12000 get_encode() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  if (!fn) {
+    cudaDriverEntryPointQueryResult q;
+    void* p = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  }
+  return fn;
+}
+
+bool logreg_tc_supported(const ModelDev& m) {
+  if (m.family != 2 || m.p > tc::BK || m.n <= 0 || m.n >= (int64_t)1 << 31) return false;
+  int dev = 0, major = 0, minor = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev);
+  cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, dev);
+  if (major != 10 || minor != 3) return false;
+  return get_encode() != nullptr;
+}
+
+cudaError_t logreg_tc_prepare(ModelDev& m, int points) {
+  tc::TCState* s = reinterpret_cast<tc::TCState*>(m.tc);
+  cudaError_t e = cudaSuccess;
+  if (!s) {
+    s = new tc::TCState();
+    m.tc = s;
+    e = cudaMalloc(&s->xb, sizeof(__nv_bfloat16) * (size_t)m.n * tc::BK);
+    if (e == cudaSuccess) e = cudaMalloc(&s->err, sizeof(int) * 2);
+    if (e != cudaSuccess) return e;
+    cudaMemset(s->err, 0, sizeof(int) * 2);
+    tc::to_bf16_kernel<<<1024, 256>>>(m.x, m.n, m.p, s->xb, s->err + 1);
+    int inexact = 0;
+    e = cudaMemcpy(&inexact, s->err + 1, sizeof(int), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return e;
+    if (inexact) return cudaErrorNotSupported;  // design matrix not exactly representable in bf16
+    cuuint64_t gdim[2] = {(cuuint64_t)tc::BK, (cuuint64_t)m.n};
+    cuuint64_t gstride[1] = {(cuuint64_t)tc::BK * 2};
+    cuuint32_t box[2] = {(cuuint32_t)tc::BK, (cuuint32_t)tc::BM};
+    cuuint32_t estride[2] = {1, 1};
+    CUresult r = get_encode()(&s->tmap, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, s->xb, gdim, gstride, box, estride,
+                              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                              CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return cudaErrorInvalidValue;
+    e = cudaFuncSetAttribute(tc::logreg_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, tc::SMEM_BYTES);
+    if (e != cudaSuccess) return e;
+    s->ok = true;
+  }
+  int blocks = (points + tc::BN - 1) / tc::BN;
+  if (blocks * tc::BN > s->bsplit_pts) {
+    cudaFree(s->bsplit);
+    s->bsplit = nullptr;
+    e = cudaMalloc(&s->bsplit, sizeof(__nv_bfloat16) * (size_t)blocks * tc::BN * tc::NSPLIT * tc::BK);
+    if (e != cudaSuccess) return e;
+    cudaMemset(s->bsplit, 0, sizeof(__nv_bfloat16) * (size_t)blocks * tc::BN * tc::NSPLIT * tc::BK);
+    s->bsplit_pts = blocks * tc::BN;
+  }
+  return e;
+}
+
+void logreg_tc_free(ModelDev& m) {
+  tc::TCState* s = reinterpret_cast<tc::TCState*>(m.tc);
+  if (!s) return;
+  cudaFree(s->xb);
+  cudaFree(s->bsplit);
+  cudaFree(s->err);
+  delete s;
+  m.tc = nullptr;
+}
+
+int logreg_tc_error(const ModelDev& m) {
+  tc::TCState* s = reinterpret_cast<tc::TCState*>(m.tc);
+  if (!s) return 0;
+  int v = 0;
+  cudaMemcpy(&v, s->err, sizeof(int), cudaMemcpyDeviceToHost);
+  return v;
+}
+
+void logreg_finish_launch(const float* Q, int npts, int ld, int p, int row_groups, const float* part_g,
+                          const double* part_ll, double prior_scale, double* PE, float* G, const int32_t* pending,
+                          cudaStream_t st);
+
+cudaError_t logreg_tc_launch(ModelDev& m, const float* Q, int npts, double* PE, float* G, const int32_t* pending,
+                             cudaStream_t st) {
+  tc::TCState* s = reinterpret_cast<tc::TCState*>(m.tc);
+  if (!s || !s->ok) return cudaErrorNotSupported;
+  cudaError_t e = logreg_tc_prepare(m, npts);
+  if (e != cudaSuccess) return e;
+  int blocks = (npts + tc::BN - 1) / tc::BN;
+  int64_t ntiles = (m.n + tc::BM - 1) / tc::BM;
+  int rg = std::max(1, 152 / blocks);
+  if (rg > ntiles) rg = (int)ntiles;
+  if (rg > m.row_groups) rg = m.row_groups;  // partial buffers are sized for m.row_groups
+  int npad = blocks * tc::BN;
+  tc::split_coefs_kernel<<<(npad * tc::BK + 255) / 256, 256, 0, st>>>(Q, npts, m.D, m.p, npad, s->bsplit, pending);
+  tc::Params P{m.y, m.n, s->bsplit, npts, rg, m.part_g, m.part_ll, s->err, pending};
+  tc::logreg_tc_kernel<<<dim3(blocks, rg), tc::NUM_THREADS, tc::SMEM_BYTES, st>>>(s->tmap, P);
+  logreg_finish_launch(Q, npts, m.D, m.p, rg, m.part_g, m.part_ll, m.hyper[0], PE, G, pending, st);
+  return cudaGetLastError();
 }
 
 }  // namespace gbn

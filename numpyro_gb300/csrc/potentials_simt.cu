@@ -509,3 +509,12 @@ cudaError_t launch_scale_rows(const double* cot, float* G, int npts, int D, cuda
 }
 
 }  // namespace gbn
+
+namespace gbn {
+void logreg_finish_launch(const float* Q, int npts, int ld, int p, int row_groups, const float* part_g,
+                          const double* part_ll, double prior_scale, double* PE, float* G, const int32_t* pending,
+                          cudaStream_t st) {
+  logreg_finish_kernel<<<(npts + 7) / 8, 256, 0, st>>>(Q, npts, ld, p, row_groups, part_g, part_ll, prior_scale, PE,
+                                                       G, pending);
+}
+}  // namespace gbn

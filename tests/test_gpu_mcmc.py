@@ -106,3 +106,21 @@ def test_large_latent_families_run(name):
     for v in samp.values():
         assert np.all(np.isfinite(v))
     assert mcmc.get_extra_fields()["accept_prob"].mean() > 0.3
+
+
+@pytest.mark.gpu
+def test_logistic_bf16x3_engine_posterior():
+    from numpyro_gb300 import _lib
+
+    if not _lib.load().gbn_tc_available():
+        pytest.skip("tcgen05 path needs an sm_103 GPU")
+    X, yv, beta = datasets.covtype_like(seed=3, n=3000, n_cont=3, n_bin=3)
+    model = models.LogisticRegression(X, yv)
+    res = {}
+    for prec in ["fp32", "bf16x3"]:
+        mcmc = MCMC(NUTS(model, precision=prec), num_warmup=300, num_samples=500, num_chains=128)
+        mcmc.run(3)
+        res[prec] = mcmc.get_samples(group_by_chain=True)["coefs"]
+    ok, m1, m2, mcse = _mcse_ok(res["bf16x3"], res["fp32"])
+    assert ok.mean() >= 0.85, (m1, m2, mcse)
+    assert np.all(diagnostics.split_gelman_rubin(res["bf16x3"]) < 1.02)

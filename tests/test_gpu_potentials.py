@@ -71,3 +71,60 @@ def test_logreg_full_size_subset_of_chains():
         assert abs(pe[c] - pr) <= 1e-7 * abs(pr) + 1e-3, (pe[c], pr)
         np.testing.assert_allclose(g[c], gr, atol=2e-3 * np.max(np.abs(gr)) + 0.05)
     k.close()
+
+
+# ---------------------------------------------------------------- tensor-core (tcgen05) logistic potential
+def _tc_or_skip():
+    from numpyro_gb300 import _lib
+
+    if not _lib.load().gbn_tc_available():
+        pytest.skip("tcgen05 path needs an sm_103 GPU")
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("n,p,C", [(1000, 13, 200), (3000, 55, 128), (257, 64, 1), (5000, 7, 1030)])
+def test_logreg_tc_matches_oracle(n, p, C):
+    """bf16x3 tensor-core potential: U within 1e-6 relative of FP64, grad within 3e-3 of its scale."""
+    _tc_or_skip()
+    from numpyro_gb300 import datasets, models
+
+    rng = np.random.default_rng(n + p)
+    X = np.empty((n, p), np.float32)
+    X[:, :-1] = datasets._round_bf16(rng.standard_normal((n, p - 1)).astype(np.float32)) if p > 1 else 0
+    X[:, -1] = 1.0
+    y = (rng.random(n) < 0.4).astype(np.float32)
+    z = (0.3 * rng.standard_normal((C, p))).astype(np.float32)
+    k = NUTS(models.LogisticRegression(X, y), num_chains=C, precision="bf16x3")
+    pe, g = k.potential_and_grad(torch.as_tensor(z, device="cuda"))
+    pe, g = pe.cpu().numpy(), g.cpu().numpy()
+    X64, y64 = X.astype(np.float64), y.astype(np.float64)
+    for c in sorted(set([0, C // 2, C - 1])):
+        pr = PR.logreg_potential(z[c], X64, y64)
+        gr = PR.logreg_grad(z[c], X64, y64)
+        assert abs(pe[c] - pr) <= 1e-6 * abs(pr) + 1e-3, (c, pe[c], pr)
+        np.testing.assert_allclose(g[c], gr, atol=3e-3 * np.max(np.abs(gr)) + 1e-3)
+    k.close()
+
+
+@pytest.mark.gpu
+def test_logreg_tc_matches_fp32_path_full_size():
+    """covtype-shaped N=581,012 x 55 with 1024 points: tensor-core vs FP32 CUDA-core potential."""
+    _tc_or_skip()
+    from numpyro_gb300 import datasets, models
+
+    X, y, beta = datasets.covtype_like(seed=0)
+    m = models.LogisticRegression(X, y)
+    rng = np.random.default_rng(1)
+    z = (beta[None, :] + 0.01 * rng.standard_normal((1024, X.shape[1]))).astype(np.float32)
+    zt = torch.as_tensor(z, device="cuda")
+    ktc = NUTS(m, num_chains=1024, precision="bf16x3")
+    k32 = NUTS(m, num_chains=1024, precision="fp32")
+    pe_tc, g_tc = [t.cpu().numpy() for t in ktc.potential_and_grad(zt)]
+    pe_32, g_32 = [t.cpu().numpy() for t in k32.potential_and_grad(zt)]
+    assert np.max(np.abs(pe_tc - pe_32) / np.abs(pe_32)) < 2e-7
+    scale = np.max(np.abs(g_32), axis=1, keepdims=True)
+    assert np.max(np.abs(g_tc - g_32) / scale) < 5e-3
+    pr = PR.logreg_potential(z[5], X.astype(np.float64), y.astype(np.float64))
+    assert abs(pe_tc[5] - pr) <= 2e-8 * abs(pr) + 0.05
+    ktc.close()
+    k32.close()
