@@ -42,8 +42,39 @@ def parse():
     p.add_argument("--iters-per-step", type=int, default=10)
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
-    p.add_argument("--cpu-seconds", type=float, default=20.0)
+    p.add_argument("--cpu-samples", type=int, default=50, help="transitions per chain of the CPU baseline")
+    p.add_argument("--plain-steps", type=int, default=3,
+                   help="steps of the plain (lock-step FP32) engine from the same adapted state; 0 = skip")
+    p.add_argument("--mode", default="nuts", choices=["nuts", "potential"],
+                   help="potential: time only the dominant kernel (U and dU for every chain)")
+    p.add_argument("--reps", type=int, default=20)
     return p.parse_args()
+
+
+def run_potential_only(args):
+    """Times the logistic potential + adjoint for all chains alone (profiling entry)."""
+    import torch
+
+    from numpyro_gb300 import NUTS, datasets, models
+
+    precision = args.precision or ("bf16x3" if _tc_available() else "fp32")
+    X, y, beta = datasets.covtype_like(seed=0, n=args.n)
+    C = args.chains
+    kernel = NUTS(models.LogisticRegression(X, y), num_chains=C, precision=precision)
+    rng = np.random.default_rng(0)
+    z = torch.as_tensor((beta[None, :] + 0.01 * rng.standard_normal((C, X.shape[1]))).astype(np.float32),
+                        device="cuda")
+    for _ in range(max(1, args.warmup)):
+        kernel.potential_and_grad(z)
+    torch.cuda.synchronize()
+    ms = _time_potential(kernel, type("S", (), {"z": z})(), reps=args.reps)
+    flop = 4.0 * X.shape[0] * X.shape[1] * C
+    burst, _, _, kind = measured_peaks()
+    print(json.dumps({"mode": "potential", "precision": precision, "n": X.shape[0], "d": X.shape[1], "chains": C,
+                      "launch_ms": ms, "tflops": flop / ms / 1e9, "frac_bf16_peak": flop / ms / 1e9 / burst,
+                      "peak_kind": kind}))
+    kernel.close()
+    return 0
 
 
 def measured_peaks():
@@ -104,57 +135,62 @@ class Clocks:
 def min_bulk_ess(z):
     from numpyro_gb300.diagnostics import bulk_effective_sample_size, split_gelman_rubin
 
+    if z.shape[1] < 4:  # split diagnostics need at least 4 draws per chain
+        return float("nan"), float("nan")
     ess = np.array([bulk_effective_sample_size(z[..., d]) for d in range(z.shape[-1])])
     rhat = np.array([split_gelman_rubin(z[..., d]) for d in range(z.shape[-1])])
     return float(ess.min()), float(np.max(rhat))
 
 
-def cpu_baseline(X, y, chains, seconds, prec="fp32"):
-    """Times the C oracle (OpenMP over chains) on a bounded sample of the workload."""
+def cpu_baseline(X, y, chains, num_samples, init=None, num_warmup=0, budget_s=0.0, prec="f32"):
+    """Times the C oracle of numpyro's NUTS (OpenMP, one chain per thread) on a bounded
+    sample of the workload: ``chains`` chains for ``num_samples`` transitions, started
+    either from an adapted state (``init`` = (z, step, inverse mass)) or from
+    init_to_uniform with a (time-bounded) Stan warmup of ``num_warmup`` iterations."""
     from oracle import build_oracle
 
     lib = build_oracle.load(prec)
     cores = len(os.sched_getaffinity(0))
-    res = build_oracle.run_logreg(lib, X, y, chains=chains, num_warmup=50, num_samples=40, seed=0,
-                                  threads=cores, budget_s=seconds)
-    from numpyro_gb300.diagnostics import bulk_effective_sample_size
-
-    z = res["samples"]
-    ess = min(bulk_effective_sample_size(z[..., d]) for d in range(z.shape[-1]))
+    res = build_oracle.run_logreg(lib, X, y, chains=chains, num_warmup=num_warmup, num_samples=num_samples,
+                                  seed=0, threads=min(cores, chains), init=init, warmup_budget_s=budget_s)
+    ess, rhat = min_bulk_ess(res["samples"])
+    start = "the GPU run's adapted state" if init is not None else \
+        "init_to_uniform + %d-iteration Stan warmup (%.0f s budget)" % (num_warmup, budget_s)
     return {
         "value": ess / res["sampling_s"],
         "unit": "ESS/s",
         "cores": res["threads"],
         "kind": "port",
         "grad_evals_per_s": res["sampling_grad_evals"] / res["sampling_s"],
-        "sample": "%d chains x (50 warmup + 40 samples) NUTS on the full N=%d x %d data, %s C oracle; "
-                  "ESS/s = min bulk-ESS of the 40 draws/chain / sampling seconds" % (
-                      res["chains"], X.shape[0], X.shape[1], prec),
+        "sampling_s": res["sampling_s"],
+        "warmup_s": res["warmup_s"],
+        "min_bulk_ess": ess,
+        "sample": "%d chains x %d NUTS transitions (max_tree_depth 10) on the full N=%d x %d data from %s; "
+                  "%s C oracle of numpyro's NUTS, one chain per host thread; ESS/s = min bulk-ESS of those "
+                  "draws / sampling seconds" % (res["chains"], num_samples, X.shape[0], X.shape[1], start, prec),
     }
 
 
 def run_reference(args):
-    """--impl reference: the oracle port of numpyro's NUTS on the host cores."""
+    """--impl reference: numpyro itself cannot run here (no jax); its NUTS algorithm runs as the
+    C oracle port on the host cores: a bounded Stan warmup, then --steps sampling steps."""
     from numpyro_gb300 import datasets
 
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return 0
     X, y, _ = datasets.covtype_like(seed=0, n=args.n)
-    steps = []
-    cb = None
-    for k in range(args.warmup + args.steps):
-        cb = cpu_baseline(X, y, chains=min(16, len(os.sched_getaffinity(0))), seconds=args.cpu_seconds)
-        if k >= args.warmup:
-            steps.append(cb)
-    value = float(np.mean([s["value"] for s in steps]))
-    line = {"metric": METRIC, "value": value, "unit": "ESS/s", "impl": "reference", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "dtype": "f32",
-            "data": "synthetic", "config": {"workload": WORKLOAD, "chains_timed": cb["cores"]},
-            "cpu_baseline": {**cb, "value": value},
-            "e2e": {"value": value, "unit": "ESS/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-            "grad_evals_per_s": float(np.mean([s["grad_evals_per_s"] for s in steps])),
-            "vs_baseline": None}
+    chains = min(16, len(os.sched_getaffinity(0)))
+    per_step = 5
+    cb = cpu_baseline(X, y, chains=chains, num_samples=max(4, args.steps * per_step), num_warmup=100,
+                      budget_s=150.0)
+    line = {"metric": METRIC, "value": cb["value"], "unit": "ESS/s", "impl": "reference", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * cb["sampling_s"] / max(1, args.steps),
+            "higher_is_better": True, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "chains_timed": chains, "iters_per_step": per_step},
+            "cpu_baseline": cb,
+            "e2e": {"value": cb["value"], "unit": "ESS/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "grad_evals_per_s": cb["grad_evals_per_s"], "vs_baseline": None}
     print(json.dumps(line))
     return 0
 
@@ -163,6 +199,8 @@ def main():
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
+    if args.mode == "potential":
+        return run_potential_only(args)
     import torch
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -242,6 +280,10 @@ def main():
     e2e = None
     if not args.no_e2e:
         e2e = _e2e(kernel, state, args.steps, B)
+    plain = None
+    if args.plain_steps > 0 and world == 1:
+        plain = _plain_compare(model, state, C, seed, args.plain_steps, B, args.num_warmup, value,
+                               grad_evals / (total_ms / 1e3))
     line = {
         "metric": METRIC, "value": value, "unit": "ESS/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": total_ms / max(1, args.steps), "higher_is_better": True,
@@ -254,12 +296,14 @@ def main():
         "min_bulk_ess": ess, "rhat_max": rhat, "warmup_s": warmup_ms / 1e3,
         "setup_s": time.perf_counter() - t0,
         "roofline": roofline, "clocks": clk, "gpu_launches": int(ticks * _launches_per_tick(precision)),
-        "e2e": e2e,
+        "e2e": e2e, "plain_engine": plain,
     }
     if rank == 0 and not args.no_cpu and world == 1:
         try:
-            line["cpu_baseline"] = cpu_baseline(X, y, chains=min(16, len(os.sched_getaffinity(0))),
-                                                seconds=args.cpu_seconds)
+            nc = min(16, len(os.sched_getaffinity(0)))
+            init = (state.z[:nc].cpu().numpy(), state.adapt_state.step_size[:nc].cpu().numpy(),
+                    state.adapt_state.inverse_mass_matrix[:nc].cpu().numpy())
+            line["cpu_baseline"] = cpu_baseline(X, y, chains=nc, num_samples=args.cpu_samples, init=init)
         except Exception as ex:  # the baseline is reported, never required for the GPU number
             line["cpu_baseline"] = {"value": None, "error": str(ex)[:200]}
     if rank == 0:
@@ -298,6 +342,46 @@ def _time_potential(kernel, state, reps=10):
         b.synchronize()
         ts.append(a.elapsed_time(b))
     return float(np.median(ts))
+
+
+def _state_leaves(st):
+    a = st.adapt_state
+    return [st.i, st.z, st.z_grad, st.potential_energy, st.energy, st.num_steps, st.accept_prob,
+            st.mean_accept_prob, st.diverging, a.step_size, a.inverse_mass_matrix, a.mass_matrix_sqrt,
+            a.mass_matrix_sqrt_inv, a.ss_state, a.mm_state[0], a.mm_state[1], a.mm_state[2], a.window_idx,
+            st.rng_key]
+
+
+def _plain_compare(model, state, C, seed, steps, B, num_warmup, fused_value, fused_gps):
+    """The plain engine (lock-step trees as under numpyro's vmap, FP32 CUDA-core potential)
+    resumed from the fused run's adapted state: same metric, same chains."""
+    import torch
+
+    from numpyro_gb300 import NUTS
+
+    k = NUTS(model, num_chains=C, engine="plain", precision="fp32")
+    st = k.init(seed, num_warmup)
+    for d, s in zip(_state_leaves(st), _state_leaves(state)):
+        d.copy_(s)
+    k.run_device(st, 1, collect=())
+    zs, ns, ms = [], [], 0.0
+    for _ in range(steps):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        out = k.run_device(st, B, collect=("z", "num_steps"))
+        b.record()
+        b.synchronize()
+        ms += a.elapsed_time(b)
+        zs.append(out["z"])
+        ns.append(out["num_steps"])
+    z = torch.cat(zs, dim=1).cpu().numpy()
+    ess, rhat = min_bulk_ess(z)
+    gps = float(torch.cat(ns, dim=1).sum().item()) / (ms / 1e3)
+    k.close()
+    return {"value": ess / (ms / 1e3), "unit": "ESS/s", "grad_evals_per_s": gps, "ms_per_step": ms / steps,
+            "steps": steps, "min_bulk_ess": ess, "rhat_max": rhat,
+            "fused_over_plain_ess_per_s": fused_value / (ess / (ms / 1e3)) if ess > 0 else None,
+            "fused_over_plain_grad_evals_per_s": fused_gps / gps}
 
 
 def _e2e(kernel, state, steps, B):

@@ -12,8 +12,10 @@
 //                            (three K=64 BF16 products accumulate in FP32 in TMEM, so the
 //                            FP32 coefficients are represented exactly: "bf16x3"),
 //                            GEMM2  G[128 chains x 64 feat] += E^T . X_tile  (E = sigmoid(L) - y)
-//   warps 2..9  epilogue: tcgen05.ld of L, sigmoid/softplus, compensated FP32 sums of the
-//               log-likelihood (warp transposed reductions), E as bf16 into shared memory.
+//   warps 2..9  epilogue: tcgen05.ld of L (software-pipelined), sigmoid/softplus with one
+//               ex2, one lg2 and one rcp per logit, E as bf16 into shared memory; the
+//               log-likelihood accumulates per thread in FP32 registers across tiles and is
+//               reduced once per CTA (lane butterfly, then FP64 across the lane quadrants).
 // L is double-buffered in TMEM (2 x 128 columns) so GEMM1 of tile t+1 overlaps the
 // epilogue of tile t; G lives in TMEM for the whole launch (64 columns).
 // The design matrix must be exactly representable in bf16 (checked on the host).
@@ -142,9 +144,133 @@ __device__ __forceinline__ float lg2_approx(float x) {
   asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
   return y;
 }
+__device__ __forceinline__ float rcp_approx(float x) {
+  float y;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
 __device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
   __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
   return *reinterpret_cast<uint32_t*>(&h);
+}
+// asynchronous TMEM load of 16 columns; the registers are valid only after tmem_wait16
+__device__ __forceinline__ void tmem_ld16u(uint32_t taddr, uint32_t (&r)[16]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+}
+// wait::ld with the loaded registers as operands, so no use can be scheduled before it
+__device__ __forceinline__ void tmem_wait16(uint32_t (&r)[16]) {
+  asm volatile("tcgen05.wait::ld.sync.aligned;"
+               : "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3]), "+r"(r[4]), "+r"(r[5]), "+r"(r[6]), "+r"(r[7]),
+                 "+r"(r[8]), "+r"(r[9]), "+r"(r[10]), "+r"(r[11]), "+r"(r[12]), "+r"(r[13]), "+r"(r[14]),
+                 "+r"(r[15])
+               :
+               : "memory");
+}
+
+// packed bf16 pair {lo, hi} (lo at the lower address)
+__device__ __forceinline__ uint32_t cvt_bf16x2(float lo, float hi) {
+  uint32_t d;
+  asm("cvt.rn.bf16x2.f32 %0, %1, %2;" : "=r"(d) : "f"(hi), "f"(lo));
+  return d;
+}
+__device__ __forceinline__ uint32_t tanh_bf16x2(uint32_t x) {
+  uint32_t y;
+  asm("tanh.approx.bf16x2 %0, %1;" : "=r"(y) : "r"(x));
+  return y;
+}
+__device__ __forceinline__ uint32_t fma_bf16x2(uint32_t a, uint32_t b, uint32_t c) {
+  uint32_t d;
+  asm("fma.rn.bf16x2 %0, %1, %2, %3;" : "=r"(d) : "r"(a), "r"(b), "r"(c));
+  return d;
+}
+
+// One tile of the epilogue for one warp: 32 rows (this lane's row) x 64 chains.
+// The accumulator holds h = l/2 (the coefficients enter GEMM1 halved, an exact scaling).
+//   sigmoid(l) - y = tanh(h)/2 + (1/2 - y)
+//   softplus(l)   = l/2 + |h| + log(1 + exp(-|l|))
+// so the per-logit log-likelihood work is |h| + log(1 + exp(-2|h|)); the linear parts
+// sum_r l_r/2 and sum_r y_r l_r are added per chain as (X^T 1 / 2 - X^T y) . b.
+// MASK zeroes rows past the end of the data.
+template <bool MASK>
+__device__ __forceinline__ void epilogue_tile(uint32_t taddr, float yv, float vmask, uint8_t* sdst, int row, int ch,
+                                              float (&acc)[64], uint32_t acc_empty_bar, int lane) {
+  const float NEG_2LOG2E = -2.8853900817779268f, LN2 = 0.6931471805599453f;
+  // (1/2 - y) as a bf16 pair; zero for rows past the data (their logits are zero, tanh(0) = 0)
+  const float c05f = (MASK && vmask == 0.0f) ? 0.0f : 0.5f - yv;
+  const uint32_t c05 = cvt_bf16x2(c05f, c05f);
+  const uint32_t half2 = 0x3F003F00u;  // (0.5, 0.5) in bf16
+  uint32_t v[2][16];
+  tmem_ld16u(taddr, v[0]);
+  tmem_wait16(v[0]);
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    if (j < 3) tmem_ld16u(taddr + 16 * (j + 1), v[(j + 1) & 1]);
+    uint32_t pk[8];
+#pragma unroll
+    for (int e = 0; e < 16; e += 2) {
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const float hl = __uint_as_float(v[j & 1][e + h]);
+        const float t = ex2_approx(fabsf(hl) * NEG_2LOG2E);  // exp(-|l|)
+        const float lg = lg2_approx(1.0f + t);               // log2(1 + exp(-|l|))
+        float llv = fmaf(LN2, lg, fabsf(hl));
+        if (MASK) llv *= vmask;
+        acc[16 * j + e + h] += llv;
+      }
+      // E = tanh(l/2)/2 + (1/2 - y) on a bf16 pair (only the gradient consumes it)
+      const uint32_t hh2 = cvt_bf16x2(__uint_as_float(v[j & 1][e]), __uint_as_float(v[j & 1][e + 1]));
+      pk[e >> 1] = fma_bf16x2(half2, tanh_bf16x2(hh2), c05);
+    }
+    // E[row][64 ch + 16 j + 0..15]: chunks 2j, 2j+1 of atom ch in the swizzled MN-major tile
+#pragma unroll
+    for (int hh = 0; hh < 2; ++hh) {
+      const int chunk = 2 * j + hh;
+      uint4 w = make_uint4(pk[4 * hh], pk[4 * hh + 1], pk[4 * hh + 2], pk[4 * hh + 3]);
+      *reinterpret_cast<uint4*>(sdst + ch * 1024 + ((chunk ^ (row & 7)) << 4)) = w;
+    }
+    if (j < 3) {
+      tmem_wait16(v[(j + 1) & 1]);
+      if (j == 2) {  // every column of this accumulator has been read: release it to the MMA warp
+        tc_fence_before();
+        __syncwarp();
+        if (lane == 0) bar_arrive(acc_empty_bar);
+      }
+    }
+  }
+}
+
+// Transposed butterfly over the 32 lanes: lane l returns the lane-sums of values 2l and 2l+1.
+__device__ __forceinline__ void warp_transpose_sum64(const float (&a)[64], float (&out)[2], int lane) {
+  float b[32], c[16], d[8], e[4];
+#pragma unroll
+  for (int i = 0; i < 32; ++i) {
+    const bool up = lane & 16;
+    b[i] = (up ? a[32 + i] : a[i]) + __shfl_xor_sync(0xffffffffu, up ? a[i] : a[32 + i], 16);
+  }
+#pragma unroll
+  for (int i = 0; i < 16; ++i) {
+    const bool up = lane & 8;
+    c[i] = (up ? b[16 + i] : b[i]) + __shfl_xor_sync(0xffffffffu, up ? b[i] : b[16 + i], 8);
+  }
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    const bool up = lane & 4;
+    d[i] = (up ? c[8 + i] : c[i]) + __shfl_xor_sync(0xffffffffu, up ? c[i] : c[8 + i], 4);
+  }
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const bool up = lane & 2;
+    e[i] = (up ? d[4 + i] : d[i]) + __shfl_xor_sync(0xffffffffu, up ? d[i] : d[4 + i], 2);
+  }
+#pragma unroll
+  for (int i = 0; i < 2; ++i) {
+    const bool up = lane & 1;
+    out[i] = (up ? e[2 + i] : e[i]) + __shfl_xor_sync(0xffffffffu, up ? e[i] : e[2 + i], 1);
+  }
 }
 
 struct Params {
@@ -294,110 +420,42 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) logreg_tc_kernel(const __grid_
     const int q = warp & 3;         // TMEM lane quadrant this warp may access
     const int ch = ew >> 2;         // column half: chains [64*ch, 64*ch+64)
     const int row = q * 32 + lane;  // row within the tile
-    float kah_s[4] = {0.f, 0.f, 0.f, 0.f}, kah_c[4] = {0.f, 0.f, 0.f, 0.f};
-    const float LOG2E = 1.4426950408889634f, LN2 = 0.6931471805599453f;
+    // log-likelihood partials of the warp's 64 chains for this lane's row slot, over all tiles
+    float acc[64];
+#pragma unroll
+    for (int k = 0; k < 64; ++k) acc[k] = 0.0f;
+    const uint32_t tl = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(ch * 64);
     bool ok = true;
+    float y_next = 0.0f;
+    if (my_tiles > 0 && (int64_t)rg * BM + row < P.n) y_next = P.y[(int64_t)rg * BM + row];
     for (int i = 0; i < my_tiles && ok; ++i) {
       const int b = i & 1;
-      const int64_t grow = ((int64_t)rg + (int64_t)i * P.row_groups) * BM + row;
-      const bool valid = grow < P.n;
-      const float yv = valid ? P.y[grow] : 0.0f;
+      const int64_t row0 = ((int64_t)rg + (int64_t)i * P.row_groups) * BM;
+      const float yv = y_next;
+      if (i + 1 < my_tiles) {
+        const int64_t gn = row0 + (int64_t)P.row_groups * BM + row;
+        y_next = gn < P.n ? P.y[gn] : 0.0f;
+      }
       ok = bar_wait(bar(B_ACCF + b), (i >> 1) & 1, abort_flag, P.err);
       if (ok && i >= 2) ok = bar_wait(bar(B_SE + b), ((i >> 1) - 1) & 1, abort_flag, P.err);
       if (!ok) break;
       tc_fence_after();
       uint8_t* sdst = smem + OFF_S + b * S_TILE + (row >> 3) * 2048 + (row & 7) * 128;
-#pragma unroll 1
-      for (int j = 0; j < 4; ++j) {
-        const int col = ch * 64 + j * 16;
-        float v[16];
-        tmem_ld16(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(b * BN + col), v);
-        tmem_wait_ld();
-        if (j == 3) {
-          tc_fence_before();
-          __syncwarp();
-          if (lane == 0) bar_arrive(bar(B_ACCE + b));
-        }
-        float ll[16];
-        uint32_t pk[8];
-#pragma unroll
-        for (int e = 0; e < 16; e += 2) {
-          float ev[2];
-#pragma unroll
-          for (int h = 0; h < 2; ++h) {
-            const float l = v[e + h];
-            const float t = ex2_approx(-fabsf(l) * LOG2E);  // exp(-|l|)
-            const float u = 1.0f + t;
-            const float lg = lg2_approx(u);                // log2(1 + exp(-|l|))
-            // 1/u by Newton-Raphson from the linear estimate 24/17 - 8/17 u on [1, 2]
-            float r = fmaf(-0.47058823529411764f, u, 1.4117647058823530f);
-            float er = fmaf(-u, r, 1.0f);
-            r = fmaf(r, er, r);
-            er = fmaf(-u, r, 1.0f);
-            r = fmaf(r, er, r);
-            const float sig = (l >= 0.0f) ? r : t * r;
-            const float sp = fmaxf(l, 0.0f) + lg * LN2;
-            ll[e + h] = valid ? fmaf(-yv, l, sp) : 0.0f;
-            ev[h] = valid ? (sig - yv) : 0.0f;
-          }
-          pk[e >> 1] = pack_bf16(ev[0], ev[1]);
-        }
-        // E[row][col..col+15] -> two 16-byte chunks of the swizzled MN-major tile
-#pragma unroll
-        for (int hh = 0; hh < 2; ++hh) {
-          const int c8 = (col >> 3) + hh;  // 8-chain chunk index in [0,16)
-          const int atom = c8 >> 3, chunk = c8 & 7;
-          uint4 w = make_uint4(pk[4 * hh], pk[4 * hh + 1], pk[4 * hh + 2], pk[4 * hh + 3]);
-          *reinterpret_cast<uint4*>(sdst + atom * 1024 + ((chunk ^ (row & 7)) << 4)) = w;
-        }
-        // transposed butterfly: lane l ends with the 32-row sum of chain col + (l >> 1)
-#pragma unroll
-        for (int i8 = 0; i8 < 8; ++i8) {
-          const bool up = lane & 16;
-          float mine = up ? ll[8 + i8] : ll[i8];
-          float give = up ? ll[i8] : ll[8 + i8];
-          ll[i8] = mine + __shfl_xor_sync(0xffffffffu, give, 16);
-        }
-#pragma unroll
-        for (int i4 = 0; i4 < 4; ++i4) {
-          const bool up = lane & 8;
-          float mine = up ? ll[4 + i4] : ll[i4];
-          float give = up ? ll[i4] : ll[4 + i4];
-          ll[i4] = mine + __shfl_xor_sync(0xffffffffu, give, 8);
-        }
-#pragma unroll
-        for (int i2 = 0; i2 < 2; ++i2) {
-          const bool up = lane & 4;
-          float mine = up ? ll[2 + i2] : ll[i2];
-          float give = up ? ll[i2] : ll[2 + i2];
-          ll[i2] = mine + __shfl_xor_sync(0xffffffffu, give, 4);
-        }
-        {
-          const bool up = lane & 2;
-          float mine = up ? ll[1] : ll[0];
-          float give = up ? ll[0] : ll[1];
-          ll[0] = mine + __shfl_xor_sync(0xffffffffu, give, 2);
-        }
-        ll[0] += __shfl_xor_sync(0xffffffffu, ll[0], 1);
-        // compensated (Kahan) accumulation across tiles
-        {
-          float yk = ll[0] - kah_c[j];
-          float tk = kah_s[j] + yk;
-          kah_c[j] = (tk - kah_s[j]) - yk;
-          kah_s[j] = tk;
-        }
-      }
+      if (row0 + BM <= P.n)
+        epilogue_tile<false>(tl + (uint32_t)(b * BN), yv, 1.0f, sdst, row, ch, acc, bar(B_ACCE + b), lane);
+      else
+        epilogue_tile<true>(tl + (uint32_t)(b * BN), yv, (row0 + row < P.n) ? 1.0f : 0.0f, sdst, row, ch, acc,
+                            bar(B_ACCE + b), lane);
       fence_proxy_async();
       __syncwarp();
       if (lane == 0) bar_arrive(bar(B_SF + b));
     }
-    // per-chain log-likelihood of this CTA's rows
-    if (ok && (lane & 1) == 0) {
-#pragma unroll
-      for (int j = 0; j < 4; ++j) {
-        const int c = ch * 64 + j * 16 + (lane >> 1);
-        atomicAdd(&ll_smem[c], (double)kah_s[j] - (double)kah_c[j]);
-      }
+    // per-chain sums over the CTA's rows: butterfly over lanes, then the four lane quadrants
+    if (ok) {
+      float s2[2];
+      warp_transpose_sum64(acc, s2, lane);
+      atomicAdd(&ll_smem[ch * 64 + 2 * lane], (double)s2[0]);
+      atomicAdd(&ll_smem[ch * 64 + 2 * lane + 1], (double)s2[1]);
     }
     // gradient partials: G (lanes = chains, 64 feature columns)
     if (ok) ok = bar_wait(bar(B_DONE), 0, abort_flag, P.err);
@@ -440,7 +498,7 @@ __global__ void split_coefs_kernel(const float* __restrict__ Q, int npts, int ld
   int idx = blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= npad * BK) return;
   int c = idx / BK, d = idx % BK;
-  float v = (c < npts && d < p) ? Q[(size_t)c * ld + d] : 0.0f;
+  float v = (c < npts && d < p) ? 0.5f * Q[(size_t)c * ld + d] : 0.0f;  // halved: the kernel works with l/2
   __nv_bfloat16 hi = __float2bfloat16_rn(v);
   float r1 = v - __bfloat162float(hi);
   __nv_bfloat16 mid = __float2bfloat16_rn(r1);
@@ -465,7 +523,22 @@ __global__ void to_bf16_kernel(const float* __restrict__ x, int64_t n, int p, __
   }
 }
 
+// lin[d] = sum_r (1/2 - y_r) X_rd in FP64 (the linear part of the log-likelihood)
+__global__ void linear_term_kernel(const float* __restrict__ x, const float* __restrict__ y, int64_t n, int p,
+                                   double* __restrict__ lin) {
+  __shared__ double part[4][64];
+  const int d = threadIdx.x & 63, rl = threadIdx.x >> 6;
+  double s = 0.0;
+  if (d < p)
+    for (int64_t r = (int64_t)blockIdx.x * 4 + rl; r < n; r += (int64_t)gridDim.x * 4)
+      s += (0.5 - (double)y[r]) * (double)x[r * p + d];
+  part[rl][d] = s;
+  __syncthreads();
+  if (rl == 0 && d < p) atomicAdd(&lin[d], part[0][d] + part[1][d] + part[2][d] + part[3][d]);
+}
+
 struct TCState {
+  double* lin = nullptr;
   __nv_bfloat16* xb = nullptr;
   __nv_bfloat16* bsplit = nullptr;
   CUtensorMap tmap;
@@ -516,6 +589,10 @@ cudaError_t logreg_tc_prepare(ModelDev& m, int points) {
     e = cudaMemcpy(&inexact, s->err + 1, sizeof(int), cudaMemcpyDeviceToHost);
     if (e != cudaSuccess) return e;
     if (inexact) return cudaErrorNotSupported;  // design matrix not exactly representable in bf16
+    e = cudaMalloc(&s->lin, sizeof(double) * tc::BK);
+    if (e != cudaSuccess) return e;
+    cudaMemset(s->lin, 0, sizeof(double) * tc::BK);
+    tc::linear_term_kernel<<<1024, 256>>>(m.x, m.y, m.n, m.p, s->lin);
     cuuint64_t gdim[2] = {(cuuint64_t)tc::BK, (cuuint64_t)m.n};
     cuuint64_t gstride[1] = {(cuuint64_t)tc::BK * 2};
     cuuint32_t box[2] = {(cuuint32_t)tc::BK, (cuuint32_t)tc::BM};
@@ -544,6 +621,7 @@ void logreg_tc_free(ModelDev& m) {
   tc::TCState* s = reinterpret_cast<tc::TCState*>(m.tc);
   if (!s) return;
   cudaFree(s->xb);
+  cudaFree(s->lin);
   cudaFree(s->bsplit);
   cudaFree(s->err);
   delete s;
@@ -559,8 +637,8 @@ int logreg_tc_error(const ModelDev& m) {
 }
 
 void logreg_finish_launch(const float* Q, int npts, int ld, int p, int row_groups, const float* part_g,
-                          const double* part_ll, double prior_scale, double* PE, float* G, const int32_t* pending,
-                          cudaStream_t st);
+                          const double* part_ll, const double* lin, double prior_scale, double* PE, float* G,
+                          const int32_t* pending, cudaStream_t st);
 
 cudaError_t logreg_tc_launch(ModelDev& m, const float* Q, int npts, double* PE, float* G, const int32_t* pending,
                              cudaStream_t st) {
@@ -577,7 +655,7 @@ cudaError_t logreg_tc_launch(ModelDev& m, const float* Q, int npts, double* PE, 
   tc::split_coefs_kernel<<<(npad * tc::BK + 255) / 256, 256, 0, st>>>(Q, npts, m.D, m.p, npad, s->bsplit, pending);
   tc::Params P{m.y, m.n, s->bsplit, npts, rg, m.part_g, m.part_ll, s->err, pending};
   tc::logreg_tc_kernel<<<dim3(blocks, rg), tc::NUM_THREADS, tc::SMEM_BYTES, st>>>(s->tmap, P);
-  logreg_finish_launch(Q, npts, m.D, m.p, rg, m.part_g, m.part_ll, m.hyper[0], PE, G, pending, st);
+  logreg_finish_launch(Q, npts, m.D, m.p, rg, m.part_g, m.part_ll, s->lin, m.hyper[0], PE, G, pending, st);
   return cudaGetLastError();
 }
 

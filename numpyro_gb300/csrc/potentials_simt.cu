@@ -193,10 +193,11 @@ __global__ void __launch_bounds__(256) logreg_simt_kernel(const float* __restric
 }
 
 // sum partials, add the N(0, scale) prior; warp per point
+// lin (optional, FP64 [p]): a linear term lin . b of the log-likelihood computed outside the kernel
 __global__ void logreg_finish_kernel(const float* __restrict__ Q, int npts, int ld, int p, int row_groups,
                                      const float* __restrict__ part_g, const double* __restrict__ part_ll,
-                                     double prior_scale, double* __restrict__ PE, float* __restrict__ G,
-                                     const int32_t* pending) {
+                                     const double* __restrict__ lin, double prior_scale, double* __restrict__ PE,
+                                     float* __restrict__ G, const int32_t* pending) {
   if (pending && *pending == 0) return;
   int c = blockIdx.x * 8 + (threadIdx.x >> 5);
   int lane = threadIdx.x & 31;
@@ -209,6 +210,7 @@ __global__ void logreg_finish_kernel(const float* __restrict__ Q, int npts, int 
     for (int r = 0; r < row_groups; ++r) s += (double)part_g[((size_t)r * npts + c) * 64 + d];
     G[(size_t)c * ld + d] = (float)(s + b * inv_var);
     lp += 0.5 * b * b * inv_var;
+    if (lin) lp += lin[d] * b;
   }
   double ll = 0.0;
   for (int r = lane; r < row_groups; r += 32) ll += part_ll[(size_t)r * npts + c];
@@ -469,7 +471,7 @@ cudaError_t launch_potential(ModelDev& m, const float* Q, int npts, double* PE, 
       logreg_simt_kernel<<<grid, 256, sm, st>>>(m.x, m.y, m.n, m.p, DP, Q, npts, ld, m.part_g, m.part_ll,
                                                 m.row_groups, pending);
       logreg_finish_kernel<<<(npts + 7) / 8, 256, 0, st>>>(Q, npts, ld, m.p, m.row_groups, m.part_g, m.part_ll,
-                                                           m.hyper[0], PE, G, pending);
+                                                           nullptr, m.hyper[0], PE, G, pending);
       break;
     }
     case 3: {
@@ -512,9 +514,9 @@ cudaError_t launch_scale_rows(const double* cot, float* G, int npts, int D, cuda
 
 namespace gbn {
 void logreg_finish_launch(const float* Q, int npts, int ld, int p, int row_groups, const float* part_g,
-                          const double* part_ll, double prior_scale, double* PE, float* G, const int32_t* pending,
-                          cudaStream_t st) {
-  logreg_finish_kernel<<<(npts + 7) / 8, 256, 0, st>>>(Q, npts, ld, p, row_groups, part_g, part_ll, prior_scale, PE,
-                                                       G, pending);
+                          const double* part_ll, const double* lin, double prior_scale, double* PE, float* G,
+                          const int32_t* pending, cudaStream_t st) {
+  logreg_finish_kernel<<<(npts + 7) / 8, 256, 0, st>>>(Q, npts, ld, p, row_groups, part_g, part_ll, lin,
+                                                       prior_scale, PE, G, pending);
 }
 }  // namespace gbn

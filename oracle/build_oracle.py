@@ -25,8 +25,11 @@ def build(force=False):
     for prec, real in (("f64", "double"), ("f32", "float")):
         path = _lib_path(prec)
         if force or not os.path.exists(path) or os.path.getmtime(path) < os.path.getmtime(SRC):
-            cmd = ["gcc", "-O3", "-fPIC", "-shared", "-fopenmp", "-std=gnu11", "-DREAL=%s" % real, SRC, "-o",
-                   path + ".tmp", "-lm"]
+            # the FP32 build (timed CPU baseline) may reassociate sums so gcc vectorises the
+            # dot products; NaN/inf semantics are kept (no -ffast-math)
+            extra = ["-fassociative-math", "-fno-signed-zeros", "-fno-trapping-math"] if real == "float" else []
+            cmd = ["gcc", "-O3", "-fPIC", "-shared", "-fopenmp", "-std=gnu11", "-DREAL=%s" % real,
+                   "-DREAL_IS_FLOAT=%d" % (real == "float")] + extra + [SRC, "-o", path + ".tmp", "-lm"]
             subprocess.check_call(cmd)
             os.replace(path + ".tmp", path)
         out.append(path)
@@ -49,7 +52,8 @@ def load(prec="f64"):
     lib.nutsref_run.restype = ctypes.c_int
     lib.nutsref_run.argtypes = [ctypes.c_int, fp, fp, fp, ctypes.c_int64, ctypes.c_int, ctypes.c_double,
                                 ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
-                                ctypes.c_uint64, ctypes.c_int, ctypes.c_int, fp, fp, fp, fp, fp, fp]
+                                ctypes.c_uint64, ctypes.c_int, ctypes.c_int, fp, fp, fp, fp, fp, fp,
+                                ctypes.c_double]
     _cache[prec] = lib
     return lib
 
@@ -59,7 +63,7 @@ def _p(a):
 
 
 def run(lib, family, X=None, y=None, sigma=None, N=0, D=0, hyper=(0.0, 0.0), chains=1, first_chain=0,
-        num_warmup=0, num_samples=0, seed=0, max_tree_depth=10, threads=0, init=None):
+        num_warmup=0, num_samples=0, seed=0, max_tree_depth=10, threads=0, init=None, warmup_budget_s=0.0):
     """init: optional (z [chains, D], step [chains], inv_mass [chains, D]) -> no adaptation."""
     samples = np.zeros((chains, max(num_samples, 0), D), np.float32)
     nsteps = np.zeros((chains, max(num_samples, 0)), np.int32)
@@ -72,17 +76,19 @@ def run(lib, family, X=None, y=None, sigma=None, N=0, D=0, hyper=(0.0, 0.0), cha
     keep = [np.ascontiguousarray(a, np.float32) if a is not None else None for a in (X, y, sigma)]
     lib.nutsref_run(family, _p(keep[0]), _p(keep[1]), _p(keep[2]), int(N), int(D), float(hyper[0]),
                     float(hyper[1]), chains, first_chain, num_warmup, num_samples, int(seed), max_tree_depth,
-                    threads, _p(iz), _p(istep), _p(iinv), _p(samples), _p(nsteps), _p(timing))
+                    threads, _p(iz), _p(istep), _p(iinv), _p(samples), _p(nsteps), _p(timing),
+                    float(warmup_budget_s))
     return {"samples": samples, "num_steps": nsteps, "warmup_s": timing[0], "sampling_s": timing[1],
             "warmup_grad_evals": timing[2], "sampling_grad_evals": timing[3], "threads": int(timing[4]),
             "chains": chains}
 
 
-def run_logreg(lib, X, y, chains, num_warmup, num_samples, seed=0, threads=0, init=None, first_chain=0):
+def run_logreg(lib, X, y, chains, num_warmup, num_samples, seed=0, threads=0, init=None, first_chain=0,
+               warmup_budget_s=0.0):
     X = np.ascontiguousarray(X, np.float32)
     return run(lib, 2, X=X, y=y, N=X.shape[0], D=X.shape[1], hyper=(1.0, 0.0), chains=chains,
                first_chain=first_chain, num_warmup=num_warmup, num_samples=num_samples, seed=seed,
-               threads=threads, init=init)
+               threads=threads, init=init, warmup_budget_s=warmup_budget_s)
 
 
 def run_hier(lib, y, sigma, chains, num_warmup, num_samples, seed=0, threads=0):

@@ -26,6 +26,9 @@
 #ifndef REAL
 #define REAL double
 #endif
+#ifndef REAL_IS_FLOAT
+#define REAL_IS_FLOAT 0
+#endif
 typedef REAL real;
 
 /* ------------------------------------------------------------------ Philox */
@@ -80,22 +83,40 @@ typedef struct {
 
 /* numpyro potential_energy of the logistic model (examples/covtype.py:66-71):
  * one fused pass over the rows; per-row arithmetic in `real`, sums in double. */
+#define LR_BLOCK 256
 static double logreg_pg(const model_t* m, const real* b, real* g) {
   int D = m->D;
   double ll = 0.0;
   double* ga = (double*)calloc((size_t)D, sizeof(double));
-  for (int64_t n = 0; n < m->N; ++n) {
-    const float* x = m->X + n * D;
-    real l = 0;
-    for (int d = 0; d < D; ++d) l += (real)x[d] * b[d];
-    real t = (real)exp(-fabs((double)l));
-    real sp = (l > 0 ? l : (real)0) + (real)log1p((double)t);
-    real sig = l >= 0 ? (real)1 / ((real)1 + t) : t / ((real)1 + t);
-    real yy = (real)m->y[n];
-    ll += (double)(sp - yy * l);
-    real e = sig - yy;
-    for (int d = 0; d < D; ++d) ga[d] += (double)(e * (real)x[d]);
+  real* gb = (real*)calloc((size_t)D, sizeof(real));
+  for (int64_t n0 = 0; n0 < m->N; n0 += LR_BLOCK) {
+    int64_t n1 = n0 + LR_BLOCK < m->N ? n0 + LR_BLOCK : m->N;
+    real llb = 0;
+    for (int64_t n = n0; n < n1; ++n) {
+      const float* x = m->X + n * D;
+      real l = 0;
+      for (int d = 0; d < D; ++d) l += (real)x[d] * b[d];
+#if REAL_IS_FLOAT
+      real t = expf(-fabsf(l));
+      real sp = (l > 0 ? l : 0.0f) + log1pf(t);
+#else
+      real t = exp(-fabs(l));
+      real sp = (l > 0 ? l : 0.0) + log1p(t);
+#endif
+      real sig = l >= 0 ? (real)1 / ((real)1 + t) : t / ((real)1 + t);
+      real yy = (real)m->y[n];
+      llb += sp - yy * l;
+      real e = sig - yy;
+      for (int d = 0; d < D; ++d) gb[d] += e * (real)x[d];
+    }
+    /* block partial sums (<= 256 rows) are flushed into double accumulators */
+    ll += (double)llb;
+    for (int d = 0; d < D; ++d) {
+      ga[d] += (double)gb[d];
+      gb[d] = 0;
+    }
   }
+  free(gb);
   double pr = 0.0, s = m->hyper[0] > 0 ? m->hyper[0] : 1.0;
   for (int d = 0; d < D; ++d) {
     g[d] = (real)(ga[d] + (double)b[d] / (s * s));
@@ -326,7 +347,8 @@ static double now_s(void) {
 int nutsref_run(int family, const float* X, const float* y, const float* sigma, int64_t N, int D, double h0,
                 double h1, int chains, int first_chain, int num_warmup, int num_samples, uint64_t seed,
                 int max_tree_depth, int threads, const float* init_z, const float* init_step,
-                const float* init_inv, float* samples, int32_t* num_steps_out, double* timing) {
+                const float* init_inv, float* samples, int32_t* num_steps_out, double* timing,
+                double warmup_budget_s) {
   model_t m = {family, N, D, X, y, sigma, {h0, h1, 0, 0}};
   seed_t s = {(uint32_t)(seed & 0xffffffffu), (uint32_t)(seed >> 32)};
   int ends[64];
@@ -377,6 +399,8 @@ int nutsref_run(int family, const float* X, const float* y, const float* sigma, 
     for (int t = 0; t < num_warmup; ++t) {
       int ns, dv;
       double ap;
+      /* a bounded baseline may cut the warmup short; it is reported as such */
+      if (warmup_budget_s > 0 && now_s() - tw0 > warmup_budget_s) break;
       nuts_transition(&m, c, s, chain, (uint32_t)t, max_tree_depth, &ns, &ap, &dv);
       if (!init_z) adapt(c, t, ap, num_warmup, ends, nwin);
     }
