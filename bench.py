@@ -77,6 +77,15 @@ def run_potential_only(args):
     return 0
 
 
+_T0 = time.perf_counter()
+
+
+def log(msg):
+    """Phase progress on stderr (the JSON result line goes to stdout)."""
+    sys.stderr.write("[bench %7.1fs] %s\n" % (time.perf_counter() - _T0, msg))
+    sys.stderr.flush()
+
+
 def measured_peaks():
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(path):
@@ -221,6 +230,7 @@ def main():
     kernel = NUTS(model, num_chains=C, engine=args.engine, precision=precision)
     seed = 1000 + rank  # replicas: independent chains per rank
     t0 = time.perf_counter()
+    log("init %d chains, precision %s" % (C, precision))
     state = kernel.init(seed, args.num_warmup)
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     ev0.record()
@@ -235,6 +245,7 @@ def main():
     torch.cuda.synchronize()
     # ---------------- timed region (device-resident inputs)
     clocks = Clocks(local)
+    log("warmup done (%.1f s); timed steps" % (warmup_ms / 1e3))
     clocks.start()
     ticks0 = kernel.stats()["ticks"]
     zs, nsteps, step_ms = [], [], []
@@ -268,6 +279,7 @@ def main():
         total_ms, ess, grad_evals = float(tmax[0]), float(t[1]), int(t[2])
     value = ess / (total_ms / 1e3)
     # ---------------- dominant kernel: the potential, timed alone on the same stream
+    log("timed steps done: %.1f ms/step" % (total_ms / max(1, args.steps)))
     pot_ms = _time_potential(kernel, state, reps=10)
     burst, sustained, hbm, peak_kind = measured_peaks()
     flop = 4.0 * X.shape[0] * X.shape[1] * C
@@ -279,9 +291,11 @@ def main():
     # ---------------- end to end through the public API with host buffers
     e2e = None
     if not args.no_e2e:
+        log("e2e")
         e2e = _e2e(kernel, state, args.steps, B)
     plain = None
     if args.plain_steps > 0 and world == 1:
+        log("plain engine comparison")
         plain = _plain_compare(model, state, C, seed, args.plain_steps, B, args.num_warmup, value,
                                grad_evals / (total_ms / 1e3))
     line = {
@@ -303,6 +317,7 @@ def main():
             nc = min(16, len(os.sched_getaffinity(0)))
             init = (state.z[:nc].cpu().numpy(), state.adapt_state.step_size[:nc].cpu().numpy(),
                     state.adapt_state.inverse_mass_matrix[:nc].cpu().numpy())
+            log("cpu baseline")
             line["cpu_baseline"] = cpu_baseline(X, y, chains=nc, num_samples=args.cpu_samples, init=init)
         except Exception as ex:  # the baseline is reported, never required for the GPU number
             line["cpu_baseline"] = {"value": None, "error": str(ex)[:200]}

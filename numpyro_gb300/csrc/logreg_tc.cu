@@ -171,21 +171,10 @@ __device__ __forceinline__ void tmem_wait16(uint32_t (&r)[16]) {
                : "memory");
 }
 
-// packed bf16 pair {lo, hi} (lo at the lower address)
-__device__ __forceinline__ uint32_t cvt_bf16x2(float lo, float hi) {
-  uint32_t d;
-  asm("cvt.rn.bf16x2.f32 %0, %1, %2;" : "=r"(d) : "f"(hi), "f"(lo));
-  return d;
-}
-__device__ __forceinline__ uint32_t tanh_bf16x2(uint32_t x) {
-  uint32_t y;
-  asm("tanh.approx.bf16x2 %0, %1;" : "=r"(y) : "r"(x));
+__device__ __forceinline__ float tanh_approx(float x) {
+  float y;
+  asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
   return y;
-}
-__device__ __forceinline__ uint32_t fma_bf16x2(uint32_t a, uint32_t b, uint32_t c) {
-  uint32_t d;
-  asm("fma.rn.bf16x2 %0, %1, %2, %3;" : "=r"(d) : "r"(a), "r"(b), "r"(c));
-  return d;
 }
 
 // One tile of the epilogue for one warp: 32 rows (this lane's row) x 64 chains.
@@ -199,10 +188,8 @@ template <bool MASK>
 __device__ __forceinline__ void epilogue_tile(uint32_t taddr, float yv, float vmask, uint8_t* sdst, int row, int ch,
                                               float (&acc)[64], uint32_t acc_empty_bar, int lane) {
   const float NEG_2LOG2E = -2.8853900817779268f, LN2 = 0.6931471805599453f;
-  // (1/2 - y) as a bf16 pair; zero for rows past the data (their logits are zero, tanh(0) = 0)
-  const float c05f = (MASK && vmask == 0.0f) ? 0.0f : 0.5f - yv;
-  const uint32_t c05 = cvt_bf16x2(c05f, c05f);
-  const uint32_t half2 = 0x3F003F00u;  // (0.5, 0.5) in bf16
+  // 1/2 - y; zero for rows past the data (their logits are zero and tanh(0) = 0)
+  const float c05 = (MASK && vmask == 0.0f) ? 0.0f : 0.5f - yv;
   uint32_t v[2][16];
   tmem_ld16u(taddr, v[0]);
   tmem_wait16(v[0]);
@@ -212,6 +199,7 @@ __device__ __forceinline__ void epilogue_tile(uint32_t taddr, float yv, float vm
     uint32_t pk[8];
 #pragma unroll
     for (int e = 0; e < 16; e += 2) {
+      float ev[2];
 #pragma unroll
       for (int h = 0; h < 2; ++h) {
         const float hl = __uint_as_float(v[j & 1][e + h]);
@@ -220,10 +208,10 @@ __device__ __forceinline__ void epilogue_tile(uint32_t taddr, float yv, float vm
         float llv = fmaf(LN2, lg, fabsf(hl));
         if (MASK) llv *= vmask;
         acc[16 * j + e + h] += llv;
+        // E = tanh(l/2)/2 + (1/2 - y) in FP32, rounded once to bf16 (rows past the data give 0)
+        ev[h] = fmaf(0.5f, tanh_approx(hl), c05);
       }
-      // E = tanh(l/2)/2 + (1/2 - y) on a bf16 pair (only the gradient consumes it)
-      const uint32_t hh2 = cvt_bf16x2(__uint_as_float(v[j & 1][e]), __uint_as_float(v[j & 1][e + 1]));
-      pk[e >> 1] = fma_bf16x2(half2, tanh_bf16x2(hh2), c05);
+      pk[e >> 1] = pack_bf16(ev[0], ev[1]);
     }
     // E[row][64 ch + 16 j + 0..15]: chunks 2j, 2j+1 of atom ch in the swizzled MN-major tile
 #pragma unroll

@@ -110,9 +110,21 @@ def rank_normalize(x):
 
 
 def bulk_effective_sample_size(x):
-    """Rank-normalised split-chain ESS ("bulk-ESS")."""
-    x = np.asarray(x, np.float64)
-    return effective_sample_size(rank_normalize(_split_chains(x)))
+    """Rank-normalised split-chain ESS ("bulk-ESS", Vehtari et al. 2021).
+
+    The autocorrelation sum follows effective_sample_size (Geyer's initial
+    monotone sequence); as in Vehtari et al. the integrated autocorrelation
+    time is bounded below by 1/log10(total draws), which keeps antithetic
+    (negatively autocorrelated) NUTS draws from short chains finite and
+    positive."""
+    z = rank_normalize(_split_chains(np.asarray(x, np.float64)))
+    total = np.prod(z.shape[:2])
+    ess = effective_sample_size(z)
+    tau = total / ess
+    floor = 1.0 / np.log10(total)
+    # a non-positive Geyer sum means antithetic draws beyond what the chains can resolve
+    tau = np.where(np.isfinite(tau) & (tau > 0), np.maximum(tau, floor), floor)
+    return total / tau
 
 
 def rank_split_rhat(x):
