@@ -12,7 +12,8 @@
 //                            (three K=64 BF16 products accumulate in FP32 in TMEM, so the
 //                            FP32 coefficients are represented exactly: "bf16x3"),
 //                            GEMM2  G[128 chains x 64 feat] += E^T . X_tile  (E = sigmoid(L) - y)
-//   warps 2..9  epilogue: tcgen05.ld of L (software-pipelined), sigmoid/softplus with one
+//   warps 2..17 epilogue (4 per TMEM lane quadrant, 32 chains each): tcgen05.ld of L
+//               (software-pipelined), sigmoid/softplus with one
 //               ex2, one lg2 and one rcp per logit, E as bf16 into shared memory; the
 //               log-likelihood accumulates per thread in FP32 registers across tiles and is
 //               reduced once per CTA (lane butterfly, then FP64 across the lane quadrants).
@@ -48,7 +49,10 @@ constexpr int OFF_S = OFF_B + NSPLIT * B_TILE;
 constexpr int OFF_MISC = OFF_S + 2 * S_TILE;
 constexpr int NUM_BARS = 2 * STAGES + 2 + 2 + 2 + 2 + 1;
 constexpr int SMEM_BYTES = OFF_MISC + 256 + BN * 8 + 1024;  // + alignment slack
-constexpr int NUM_THREADS = 320;
+constexpr int EPI_WARPS = 16;             // epilogue warps: 4 per TMEM lane quadrant
+constexpr int CW = BN * 4 / EPI_WARPS;    // chains per epilogue warp
+constexpr int GCOLS = BK * 4 / EPI_WARPS; // gradient columns read back per epilogue warp
+constexpr int NUM_THREADS = 32 * (2 + EPI_WARPS);
 constexpr uint32_t TMEM_COLS = 512;
 constexpr uint32_t ACC2_COL = 256;
 constexpr uint32_t WAIT_LIMIT = 1u << 22;
@@ -184,18 +188,25 @@ __device__ __forceinline__ float tanh_approx(float x) {
 // so the per-logit log-likelihood work is |h| + log(1 + exp(-2|h|)); the linear parts
 // sum_r l_r/2 and sum_r y_r l_r are added per chain as (X^T 1 / 2 - X^T y) . b.
 // MASK zeroes rows past the end of the data.
-template <bool MASK>
-__device__ __forceinline__ void epilogue_tile(uint32_t taddr, float yv, float vmask, uint8_t* sdst, int row, int ch,
-                                              float (&acc)[64], uint32_t acc_empty_bar, int lane) {
+// The warp covers CW chains starting at column col0 of the tile (CW a multiple of 16).
+template <bool MASK, int CW>
+__device__ __forceinline__ void epilogue_tile(uint32_t taddr, float yv, float vmask, uint8_t* sdst, int row, int col0,
+                                              float (&acc)[CW], uint32_t acc_empty_bar, int lane) {
+  constexpr int NCH = CW / 16;
   const float NEG_2LOG2E = -2.8853900817779268f, LN2 = 0.6931471805599453f;
   // 1/2 - y; zero for rows past the data (their logits are zero and tanh(0) = 0)
   const float c05 = (MASK && vmask == 0.0f) ? 0.0f : 0.5f - yv;
   uint32_t v[2][16];
   tmem_ld16u(taddr, v[0]);
   tmem_wait16(v[0]);
+  if (NCH == 1) {  // every column of this accumulator has been read: release it to the MMA warp
+    tc_fence_before();
+    __syncwarp();
+    if (lane == 0) bar_arrive(acc_empty_bar);
+  }
 #pragma unroll
-  for (int j = 0; j < 4; ++j) {
-    if (j < 3) tmem_ld16u(taddr + 16 * (j + 1), v[(j + 1) & 1]);
+  for (int j = 0; j < NCH; ++j) {
+    if (j + 1 < NCH) tmem_ld16u(taddr + 16 * (j + 1), v[(j + 1) & 1]);
     uint32_t pk[8];
 #pragma unroll
     for (int e = 0; e < 16; e += 2) {
@@ -213,16 +224,16 @@ __device__ __forceinline__ void epilogue_tile(uint32_t taddr, float yv, float vm
       }
       pk[e >> 1] = pack_bf16(ev[0], ev[1]);
     }
-    // E[row][64 ch + 16 j + 0..15]: chunks 2j, 2j+1 of atom ch in the swizzled MN-major tile
+    // E[row][col0 + 16 j + 0..15]: two 16-byte chunks of the swizzled MN-major tile
 #pragma unroll
     for (int hh = 0; hh < 2; ++hh) {
-      const int chunk = 2 * j + hh;
+      const int c8 = (col0 >> 3) + 2 * j + hh;  // 8-chain chunk index in [0, 16)
       uint4 w = make_uint4(pk[4 * hh], pk[4 * hh + 1], pk[4 * hh + 2], pk[4 * hh + 3]);
-      *reinterpret_cast<uint4*>(sdst + ch * 1024 + ((chunk ^ (row & 7)) << 4)) = w;
+      *reinterpret_cast<uint4*>(sdst + (c8 >> 3) * 1024 + (((c8 & 7) ^ (row & 7)) << 4)) = w;
     }
-    if (j < 3) {
+    if (j + 1 < NCH) {
       tmem_wait16(v[(j + 1) & 1]);
-      if (j == 2) {  // every column of this accumulator has been read: release it to the MMA warp
+      if (j + 2 == NCH) {  // every column of this accumulator has been read: release it to the MMA warp
         tc_fence_before();
         __syncwarp();
         if (lane == 0) bar_arrive(acc_empty_bar);
@@ -231,34 +242,24 @@ __device__ __forceinline__ void epilogue_tile(uint32_t taddr, float yv, float vm
   }
 }
 
-// Transposed butterfly over the 32 lanes: lane l returns the lane-sums of values 2l and 2l+1.
-__device__ __forceinline__ void warp_transpose_sum64(const float (&a)[64], float (&out)[2], int lane) {
-  float b[32], c[16], d[8], e[4];
+// One halving step of the transposed butterfly: lanes with bit `off` set keep the upper half.
+template <int N>
+__device__ __forceinline__ void butterfly_step(const float* a, float* b, int lane, int off) {
+  const bool up = lane & off;
 #pragma unroll
-  for (int i = 0; i < 32; ++i) {
-    const bool up = lane & 16;
-    b[i] = (up ? a[32 + i] : a[i]) + __shfl_xor_sync(0xffffffffu, up ? a[i] : a[32 + i], 16);
-  }
-#pragma unroll
-  for (int i = 0; i < 16; ++i) {
-    const bool up = lane & 8;
-    c[i] = (up ? b[16 + i] : b[i]) + __shfl_xor_sync(0xffffffffu, up ? b[i] : b[16 + i], 8);
-  }
-#pragma unroll
-  for (int i = 0; i < 8; ++i) {
-    const bool up = lane & 4;
-    d[i] = (up ? c[8 + i] : c[i]) + __shfl_xor_sync(0xffffffffu, up ? c[i] : c[8 + i], 4);
-  }
-#pragma unroll
-  for (int i = 0; i < 4; ++i) {
-    const bool up = lane & 2;
-    e[i] = (up ? d[4 + i] : d[i]) + __shfl_xor_sync(0xffffffffu, up ? d[i] : d[4 + i], 2);
-  }
-#pragma unroll
-  for (int i = 0; i < 2; ++i) {
-    const bool up = lane & 1;
-    out[i] = (up ? e[2 + i] : e[i]) + __shfl_xor_sync(0xffffffffu, up ? e[i] : e[2 + i], 1);
-  }
+  for (int i = 0; i < N / 2; ++i)
+    b[i] = (up ? a[N / 2 + i] : a[i]) + __shfl_xor_sync(0xffffffffu, up ? a[i] : a[N / 2 + i], off);
+}
+// Transposed butterfly over the 32 lanes of N values: lane l returns the lane-sums of
+// values (N/32) l + i, i < N/32.
+template <int N>
+__device__ __forceinline__ void warp_transpose_sum(const float (&a)[N], float (&out)[N / 32], int lane) {
+  float b[N / 2], c[N / 4], d[N / 8], e[N / 16];
+  butterfly_step<N>(a, b, lane, 16);
+  butterfly_step<N / 2>(b, c, lane, 8);
+  butterfly_step<N / 4>(c, d, lane, 4);
+  butterfly_step<N / 8>(d, e, lane, 2);
+  butterfly_step<N / 16>(e, out, lane, 1);
 }
 
 struct Params {
@@ -296,8 +297,8 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) logreg_tc_kernel(const __grid_
     }
     for (int i = 0; i < 2; ++i) {
       bar_init(bar(B_ACCF + i), 1);
-      bar_init(bar(B_ACCE + i), 8);
-      bar_init(bar(B_SF + i), 8);
+      bar_init(bar(B_ACCE + i), EPI_WARPS);
+      bar_init(bar(B_SF + i), EPI_WARPS);
       bar_init(bar(B_SE + i), 1);
     }
     bar_init(bar(B_DONE), 1);
@@ -403,16 +404,17 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) logreg_tc_kernel(const __grid_
       }
     }
   } else {
-    // ------------------------------------------------------------ epilogue (warps 2..9)
+    // ------------------------------------------------------------ epilogue (warps 2..17)
     const int ew = warp - 2;
     const int q = warp & 3;         // TMEM lane quadrant this warp may access
-    const int ch = ew >> 2;         // column half: chains [64*ch, 64*ch+64)
+    const int ch = ew >> 2;         // column group: chains [CW*ch, CW*ch+CW)
     const int row = q * 32 + lane;  // row within the tile
-    // log-likelihood partials of the warp's 64 chains for this lane's row slot, over all tiles
-    float acc[64];
+    const int col0 = ch * CW;       // first chain (tile column) of this warp
+    // log-likelihood partials of the warp's CW chains for this lane's row slot, over all tiles
+    float acc[CW];
 #pragma unroll
-    for (int k = 0; k < 64; ++k) acc[k] = 0.0f;
-    const uint32_t tl = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(ch * 64);
+    for (int k = 0; k < CW; ++k) acc[k] = 0.0f;
+    const uint32_t tl = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)col0;
     bool ok = true;
     float y_next = 0.0f;
     if (my_tiles > 0 && (int64_t)rg * BM + row < P.n) y_next = P.y[(int64_t)rg * BM + row];
@@ -430,20 +432,20 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) logreg_tc_kernel(const __grid_
       tc_fence_after();
       uint8_t* sdst = smem + OFF_S + b * S_TILE + (row >> 3) * 2048 + (row & 7) * 128;
       if (row0 + BM <= P.n)
-        epilogue_tile<false>(tl + (uint32_t)(b * BN), yv, 1.0f, sdst, row, ch, acc, bar(B_ACCE + b), lane);
+        epilogue_tile<false, CW>(tl + (uint32_t)(b * BN), yv, 1.0f, sdst, row, col0, acc, bar(B_ACCE + b), lane);
       else
-        epilogue_tile<true>(tl + (uint32_t)(b * BN), yv, (row0 + row < P.n) ? 1.0f : 0.0f, sdst, row, ch, acc,
-                            bar(B_ACCE + b), lane);
+        epilogue_tile<true, CW>(tl + (uint32_t)(b * BN), yv, (row0 + row < P.n) ? 1.0f : 0.0f, sdst, row, col0,
+                                acc, bar(B_ACCE + b), lane);
       fence_proxy_async();
       __syncwarp();
       if (lane == 0) bar_arrive(bar(B_SF + b));
     }
     // per-chain sums over the CTA's rows: butterfly over lanes, then the four lane quadrants
     if (ok) {
-      float s2[2];
-      warp_transpose_sum64(acc, s2, lane);
-      atomicAdd(&ll_smem[ch * 64 + 2 * lane], (double)s2[0]);
-      atomicAdd(&ll_smem[ch * 64 + 2 * lane + 1], (double)s2[1]);
+      float s[CW / 32];
+      warp_transpose_sum<CW>(acc, s, lane);
+#pragma unroll
+      for (int k = 0; k < CW / 32; ++k) atomicAdd(&ll_smem[col0 + (CW / 32) * lane + k], (double)s[k]);
     }
     // gradient partials: G (lanes = chains, 64 feature columns)
     if (ok) ok = bar_wait(bar(B_DONE), 0, abort_flag, P.err);
@@ -452,9 +454,9 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) logreg_tc_kernel(const __grid_
       const int c = q * 32 + lane;
       const int gc = cb * BN + c;
 #pragma unroll
-      for (int j = 0; j < 2; ++j) {
+      for (int j = 0; j < GCOLS / 16; ++j) {
         float v[16];
-        const int colb = ch * 32 + j * 16;
+        const int colb = ch * GCOLS + j * 16;
         tmem_ld16(tmem + ((uint32_t)(q * 32) << 16) + ACC2_COL + (uint32_t)colb, v);
         tmem_wait_ld();
         if (gc < P.npts) {
