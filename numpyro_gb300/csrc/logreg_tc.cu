@@ -13,8 +13,8 @@
 //                            FP32 coefficients are represented exactly: "bf16x3"),
 //                            GEMM2  G[128 chains x 64 feat] += E^T . X_tile  (E = sigmoid(L) - y)
 //   warps 2..17 epilogue (4 per TMEM lane quadrant, 32 chains each): tcgen05.ld of L
-//               (software-pipelined), sigmoid/softplus with one
-//               ex2, one lg2 and one rcp per logit, E as bf16 into shared memory; the
+//               (software-pipelined), sigmoid/softplus with one ex2, one lg2 and one
+//               tanh per logit (special-function bound), E as bf16 into shared memory; the
 //               log-likelihood accumulates per thread in FP32 registers across tiles and is
 //               reduced once per CTA (lane butterfly, then FP64 across the lane quadrants).
 // L is double-buffered in TMEM (2 x 128 columns) so GEMM1 of tile t+1 overlaps the
