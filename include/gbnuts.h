@@ -171,6 +171,25 @@ int gbn_run(gbn_handle h, void* stream, gbn_state* st, int32_t num_iterations,
 
 int gbn_get_stats(gbn_handle h, gbn_stats* stats);
 
+/* Largest num_points accepted by gbn_logreg_potential_noalloc. */
+#define GBN_NOALLOC_MAX_POINTS 256
+
+/* Logistic-regression U(z) and dU/dz (FP32 CUDA cores, same arithmetic as the
+ * LOGREG family) that allocates no device memory, for callers that cannot call
+ * cudaMalloc: a JAX/XLA FFI handler (XLA owns the device buffers), code running
+ * inside a CUDA stream capture, hosts that manage all memory in their own pool.
+ * No counterpart in the reference.  d_x [n][p] row-major, d_y [n], d_z
+ * [num_points][p], d_pe [num_points], d_grad [num_points][p]; requires
+ * 1 <= num_points <= GBN_NOALLOC_MAX_POINTS and 1 <= p <= 64, else
+ * GBN_ERR_INVALID_ARG.  Its scratch is a static device array of about 1 MB that
+ * every GPU loading the library holds until exit, shared by all calls: calls
+ * that overlap on the GPU race and must be serialised by the caller.  The first
+ * call on a device performs the set-up and should come before any stream capture. */
+int gbn_logreg_potential_noalloc(void* stream, const float* d_x, const float* d_y, int64_t n, int32_t p,
+                                 double prior_scale, const float* d_z, int32_t num_points, double* d_pe,
+                                 float* d_grad);
+const char* gbn_noalloc_last_error(void);
+
 #ifdef __cplusplus
 }
 #endif

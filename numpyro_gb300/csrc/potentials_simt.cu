@@ -513,6 +513,27 @@ cudaError_t launch_scale_rows(const double* cot, float* G, int npts, int D, cuda
 }  // namespace gbn
 
 namespace gbn {
+// FP32 logistic potential with scratch supplied by the caller (no allocation):
+// part_g needs row_groups * npts * 64 floats, part_ll row_groups * npts doubles.
+cudaError_t launch_logreg_simt_scratch(const float* x, const float* y, int64_t n, int p, double prior_scale,
+                                       const float* Q, int npts, int row_groups, float* part_g, double* part_ll,
+                                       double* PE, float* G, cudaStream_t st) {
+  static bool attr_set = false;
+  if (!attr_set) {
+    cudaError_t e = cudaFuncSetAttribute(logreg_simt_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)logreg_smem(64));
+    if (e != cudaSuccess) return e;
+    attr_set = true;
+  }
+  int DP = logreg_dp(p);
+  dim3 grid((npts + LR_CT - 1) / LR_CT, row_groups);
+  logreg_simt_kernel<<<grid, 256, logreg_smem(DP), st>>>(x, y, n, p, DP, Q, npts, p, part_g, part_ll, row_groups,
+                                                         nullptr);
+  logreg_finish_kernel<<<(npts + 7) / 8, 256, 0, st>>>(Q, npts, p, p, row_groups, part_g, part_ll, nullptr,
+                                                       prior_scale, PE, G, nullptr);
+  return cudaGetLastError();
+}
+
 void logreg_finish_launch(const float* Q, int npts, int ld, int p, int row_groups, const float* part_g,
                           const double* part_ll, const double* lin, double prior_scale, double* PE, float* G,
                           const int32_t* pending, cudaStream_t st) {
