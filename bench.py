@@ -48,7 +48,78 @@ def parse():
     p.add_argument("--mode", default="nuts", choices=["nuts", "potential"],
                    help="potential: time only the dominant kernel (U and dU for every chain)")
     p.add_argument("--reps", type=int, default=20)
+    p.add_argument("--workload", default="logreg",
+                   choices=["logreg", "eight_schools", "uneven_hier", "horseshoe", "sv"],
+                   help="non-default workloads: a full warmup+sampling run of that model family")
+    p.add_argument("--samples", type=int, default=None, help="sampling iterations of a --workload run")
     return p.parse_args()
+
+
+def run_workload(args):
+    """Full NUTS run (warmup + sampling, both timed with CUDA events) of one of the
+    other model families at its benchmark shape; prints one JSON line."""
+    import torch
+
+    from numpyro_gb300 import NUTS, datasets, models
+
+    w = args.workload
+    if w == "eight_schools":
+        y, s = datasets.eight_schools(0)
+        model, C, W, S = models.HierarchicalNormal(y, s), 4, 1000, 1000
+        shape = "J=8, 4 chains"
+    elif w == "uneven_hier":
+        ds = datasets.uneven_hierarchical(seed=0)
+        # 200 draws keep the collected [16384, S, 258] draws (about 3.4 GB) small enough to copy
+        model, C, W, S = models.HierarchicalNormal(datasets=ds), 4 * len(ds), 1000, 200
+        shape = "4096 datasets, J in [4,256], 16384 chains"
+    elif w == "horseshoe":
+        X, y, _ = datasets.horseshoe_data(seed=0)
+        model, C, W, S = models.HorseshoeRegression(X, y), 256, 300, 300
+        shape = "N=2000, P=1000 (D=2002), 256 chains"
+    else:
+        r, _ = datasets.sv_returns(seed=0)
+        model, C, W, S = models.StochasticVolatility(r), 256, 500, 500
+        shape = "T=4096 (D=4098), 256 chains"
+    if args.num_warmup != 500:
+        W = args.num_warmup
+    if args.samples:
+        S = args.samples
+    k = NUTS(model, num_chains=C)
+    log("%s: %s, %d warmup + %d samples" % (w, shape, W, S))
+    st = k.init(1, W)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+    ev[0].record()
+    k.run_device(st, W, collect_start=W, collect=())
+    ev[1].record()
+    t_ticks = k.stats()["ticks"]
+    out = k.run_device(st, S, collect=("z", "num_steps", "diverging"))
+    ev[2].record()
+    torch.cuda.synchronize()
+    warm_s, samp_s = ev[0].elapsed_time(ev[1]) / 1e3, ev[1].elapsed_time(ev[2]) / 1e3
+    ticks = k.stats()["ticks"] - t_ticks
+    z = out["z"].cpu().numpy()
+    ns = out["num_steps"].cpu().numpy()
+    if w == "uneven_hier":  # ESS per model over its 4 chains, padding excluded
+        Dk = np.array([model.chain_latent_dim(4 * m, 4) for m in range(model.num_models)])
+        ess, rhat = [], []
+        for m in range(0, model.num_models, 64):  # a strided sample of 64 models keeps the host work small
+            e, r = min_bulk_ess(z[4 * m:4 * m + 4, :, :Dk[m]])
+            ess.append(e)
+            rhat.append(r)
+        ess_min, rhat_max = float(np.min(ess)), float(np.max(rhat))
+        ess_note = "min over a strided sample of 64 models of the per-model min bulk-ESS"
+    else:
+        ess_min, rhat_max = min_bulk_ess(z)
+        ess_note = "min over latent coordinates"
+    line = {"workload": w, "shape": shape, "chains": C, "num_warmup": W, "num_samples": S,
+            "warmup_s": warm_s, "sampling_s": samp_s, "grad_evals_per_s_sampling": float(ns.sum()) / samp_s,
+            "mean_num_steps": float(ns.mean()), "divergences": int(out["diverging"].sum().item()),
+            "min_bulk_ess": ess_min, "min_bulk_ess_per_s_sampling": ess_min / samp_s,
+            "min_bulk_ess_per_s_total": ess_min / (warm_s + samp_s), "rhat_max": rhat_max,
+            "ess_definition": ess_note, "ticks_sampling": ticks, "us_per_tick": 1e6 * samp_s / max(1, ticks)}
+    print(json.dumps(line))
+    k.close()
+    return 0
 
 
 def run_potential_only(args):
@@ -210,6 +281,8 @@ def main():
         return run_reference(args)
     if args.mode == "potential":
         return run_potential_only(args)
+    if args.workload != "logreg":
+        return run_workload(args)
     import torch
 
     world = int(os.environ.get("WORLD_SIZE", "1"))

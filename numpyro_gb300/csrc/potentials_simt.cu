@@ -136,6 +136,7 @@ __global__ void __launch_bounds__(256) logreg_simt_kernel(const float* __restric
 #pragma unroll
         for (int j = 0; j < 4; ++j) acc[i][j] = fmaf(xa[i], ba[j], acc[i][j]);
     }
+    float llt[4] = {0.0f, 0.0f, 0.0f, 0.0f};  // this tile's 4 rows, folded into FP64 once per tile
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
       int r = ty * 4 + i;
@@ -151,10 +152,12 @@ __global__ void __launch_bounds__(256) logreg_simt_kernel(const float* __restric
         float sig = (l >= 0.0f) ? inv : t * inv;
         bool v = rv && (c0 + tx * 4 + j) < npts;
         ev[j] = v ? (sig - yy) : 0.0f;
-        if (v) llacc[j] += (double)(sp - yy * l);
+        llt[j] += v ? (sp - yy * l) : 0.0f;
       }
       *reinterpret_cast<float4*>(&Es[r * LR_CT + tx * 4]) = make_float4(ev[0], ev[1], ev[2], ev[3]);
     }
+#pragma unroll
+    for (int j = 0; j < 4; ++j) llacc[j] += (double)llt[j];
     __syncthreads();
     if (g_active) {
       for (int r = 0; r < LR_RT; ++r) {
