@@ -53,6 +53,9 @@ extern "C" {
 /* engines */
 #define GBN_ENGINE_FUSED 0 /* per-chain trees, no lock-step, fused/tensor-core potentials */
 #define GBN_ENGINE_PLAIN 1 /* lock-step masked trees (numpyro vmap semantics), FP32 CUDA-core potentials */
+#define GBN_ENGINE_TICKS 2 /* per-chain trees on the launch-per-leapfrog tick engine (no persistent kernel) */
+/* GBN_ENGINE_FUSED runs the hierarchical family in one persistent launch (warps pull chains
+ * from a device work queue); other families use the tick engine. */
 
 /* algorithms */
 #define GBN_ALGO_NUTS 0

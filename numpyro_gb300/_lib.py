@@ -21,7 +21,7 @@ ERRORS = {
 }
 
 FAMILY_HIER_NC, FAMILY_LOGREG, FAMILY_HORSESHOE, FAMILY_SV = 1, 2, 3, 4
-ENGINE_FUSED, ENGINE_PLAIN = 0, 1
+ENGINE_FUSED, ENGINE_PLAIN, ENGINE_TICKS = 0, 1, 2
 ALGO_NUTS, ALGO_HMC = 0, 1
 PREC_FP32, PREC_BF16X3 = 0, 1
 

@@ -33,6 +33,8 @@ struct gbn_handle_s {
   int32_t* flags = nullptr;
   int32_t* err_word = nullptr;
   int32_t* window_end = nullptr;
+  int persistent = 0;         // run gbn_run through the persistent engine
+  int32_t* order = nullptr;   // persistent engine: chain queue order
   int num_windows = 0;
   int num_warmup = 0;
   int initialised = 0;
@@ -279,6 +281,16 @@ int gbn_create(gbn_handle* out, const gbn_model_desc* md, const gbn_config* cfg)
     if (ce == cudaSuccess)
       ce = cudaMemcpy(e.chain_dim, chain_dim.data(), sizeof(int32_t) * C, cudaMemcpyHostToDevice);
   }
+  // persistent engine (hierarchical family, non-lock-step): chain queue ordered longest first
+  h->persistent = (m.family == GBN_FAMILY_HIER_NC && cfg->engine == GBN_ENGINE_FUSED);
+  if (ce == cudaSuccess && h->persistent) {
+    std::vector<int32_t> order(C);
+    for (int c = 0; c < C; ++c) order[c] = c;
+    if (!chain_dim.empty())
+      std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return chain_dim[a] > chain_dim[b]; });
+    ce = dalloc(h, &h->order, (size_t)C);
+    if (ce == cudaSuccess) ce = cudaMemcpy(h->order, order.data(), sizeof(int32_t) * C, cudaMemcpyHostToDevice);
+  }
   if (ce == cudaSuccess) ce = dalloc(h, &h->counters, 8);
   if (ce == cudaSuccess) ce = dalloc(h, &h->flags, (size_t)C);
   if (ce == cudaSuccess) ce = dalloc(h, &h->err_word, 4);
@@ -505,7 +517,20 @@ int gbn_run(gbn_handle h, void* stream, gbn_state* st, int32_t num_iterations, i
   if (h->cfg.find_heuristic_step_size) per_iter += 512;
   int64_t max_ticks = (int64_t)num_iterations * per_iter * (P.lockstep ? 2 : 1) + 4096;
   cudaEventRecord(h->ev0, s);
-  int r = tick_loop(h, s, max_ticks);
+  int r = GBN_OK;
+  if (h->persistent) {
+    // one launch: every chain runs all its transitions from the device work queue
+    e = cudaMemsetAsync(h->counters + 7, 0, sizeof(int32_t), s);
+    if (e != cudaSuccess) return cuda_fail(h, e, "gbn_run: queue");
+    HierView hv{h->m.y, h->m.sigma, h->m.offsets, h->m.chains_per_model, h->m.num_models, h->m.hyper[0],
+                h->m.hyper[1]};
+    launch_persistent_hier(h->dP, hv, h->counters + 7, h->order, h->C, s);
+    e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return cuda_fail(h, e, "gbn_run: persistent engine");
+  } else {
+    r = tick_loop(h, s, max_ticks);
+  }
   cudaEventRecord(h->ev1, s);
   if (r != GBN_OK) return r;
   cudaEventSynchronize(h->ev1);

@@ -32,8 +32,20 @@ struct ModelDev {
   void* tc = nullptr;         // tensor-core path state (logreg_tc.cu)
 };
 
+// device view of the hierarchical family's data (persistent engine)
+struct HierView {
+  const float* y;
+  const float* sg;
+  const int32_t* off;
+  int cpm;
+  int num_models;
+  double mu_scale, tau_scale;
+};
+
 // nuts_engine.cu
 void launch_advance(const AdvParams* dP, int C, int D, int parity, cudaStream_t st);
+void launch_persistent_hier(const AdvParams* dP, const HierView& hv, int32_t* queue_head, const int32_t* order,
+                            int C, cudaStream_t st);
 void launch_init_uniform(const AdvParams* dP, int C, int D, int attempt, const int32_t* flag, cudaStream_t st);
 void launch_check_valid(const AdvParams* dP, int C, int32_t* flag, int32_t* count, cudaStream_t st);
 void launch_init_state(const AdvParams* dP, int C, int D, const float* inv_mass_init, float init_step,

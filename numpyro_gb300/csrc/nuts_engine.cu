@@ -25,6 +25,7 @@
 // numpyro/infer/hmc.py: momentum_generator :92-110, _hmc_next :364-414,
 //   _nuts_next :416-455, sample_kernel :459-530.
 #include "common.cuh"
+#include "hier_potential.cuh"
 #include "internal.h"
 
 namespace gbn {
@@ -696,7 +697,55 @@ __global__ void set_rng_chain_kernel(uint32_t* rng_key, int C, int first_chain) 
   }
 }
 
+// --------------------------------------------------------------------- persistent engine
+// For the hierarchical family the potential costs O(J) per gradient, so a launch
+// per leapfrog step is pure overhead.  Each warp pops chains from a device work
+// queue (ordered longest-first) and runs every requested transition of its chain --
+// tree doubling, leaves, U-turn checks, adaptation, collection -- calling the
+// warp-level potential inline between state-machine steps.  Chains never wait for
+// one another; there is no grid-wide synchronisation and no spin-wait.
+__global__ void __launch_bounds__(256) persistent_hier_kernel(const AdvParams* __restrict__ Pp, HierView hv,
+                                                              int32_t* queue_head, const int32_t* __restrict__ order) {
+  const AdvParams& P = *Pp;
+  const int lane = threadIdx.x & 31;
+  for (;;) {
+    int k = 0;
+    if (lane == 0) k = atomicAdd(queue_head, 1);
+    k = __shfl_sync(0xffffffffu, k, 0);
+    if (k >= P.C) break;
+    const int c = order ? order[k] : k;
+    int m = c / hv.cpm;
+    if (m >= hv.num_models) m = hv.num_models - 1;
+    const int j0 = hv.off[m], J = hv.off[m + 1] - j0;
+    Chain<32> ch{P, Group<32>{lane}, nullptr, c, P.e.chain_dim ? P.e.chain_dim[c] : P.D, P.D, P.e.ctl[c]};
+    ch.run();
+    for (;;) {
+      const int ph = ch.ctl.phase;
+      if (!(ph == PH_LEAF || ph == PH_HMC || ph == PH_HEUR)) break;
+      __syncwarp();  // Q written by other lanes
+      hier_nc_potential_warp(P.e.Q + (size_t)c * P.D, P.e.G + (size_t)c * P.D, P.e.PE + c, J, hv.y + j0,
+                             hv.sg + j0, hv.mu_scale, hv.tau_scale, lane);
+      __syncwarp();  // G and PE written by other lanes
+      ch.run();
+    }
+    if (lane == 0) P.e.ctl[c] = ch.ctl;
+  }
+}
+
 // --------------------------------------------------------------------- launchers
+void launch_persistent_hier(const AdvParams* dP, const HierView& hv, int32_t* queue_head, const int32_t* order,
+                            int C, cudaStream_t st) {
+  int dev = 0, sms = 0, per_sm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, persistent_hier_kernel, 256, 0);
+  if (per_sm < 1) per_sm = 1;
+  int blocks = sms * per_sm;
+  int need = (C + 7) / 8;  // never more warps than chains
+  if (blocks > need) blocks = need;
+  persistent_hier_kernel<<<blocks, 256, 0, st>>>(dP, hv, queue_head, order);
+}
+
 void launch_advance(const AdvParams* dP, int C, int D, int parity, cudaStream_t st) {
   if (D <= 1024) {
     int cpb = 8;

@@ -13,6 +13,7 @@
 // relative even for 581k-row likelihoods.
 #include <cstdio>
 #include "common.cuh"
+#include "hier_potential.cuh"
 #include "internal.h"
 
 namespace gbn {
@@ -36,37 +37,8 @@ __global__ void __launch_bounds__(256) hier_nc_kernel(const float* __restrict__ 
   int m = c / cpm;
   if (m >= num_models) m = num_models - 1;  // points beyond the configured chains reuse the last model
   int j0 = off[m], J = off[m + 1] - j0;
-  const float* z = Q + (size_t)c * ld;
-  float* g = G + (size_t)c * ld;
-  float mu = z[0], lt = z[1];
-  float tau = expf(lt);
-  double lp = 0.0, sw = 0.0, swe = 0.0;
-  for (int j = lane; j < J; j += 32) {
-    float eta = z[2 + j];
-    float yy = y[j0 + j], s = sg[j0 + j];
-    float th = fmaf(tau, eta, mu);
-    float r = (yy - th) / s;
-    lp += (double)(-0.5f * eta * eta - 0.5f * r * r - logf(s));
-    float w = r / s;
-    sw += (double)w;
-    swe += (double)(w * eta);
-    g[2 + j] = eta - tau * w;
-  }
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    lp += __shfl_xor_sync(0xffffffffu, lp, o);
-    sw += __shfl_xor_sync(0xffffffffu, sw, o);
-    swe += __shfl_xor_sync(0xffffffffu, swe, o);
-  }
-  if (lane == 0) {
-    double dmu = (double)mu, dt = exp((double)lt);
-    double lp_mu = -0.5 * (dmu / mu_scale) * (dmu / mu_scale) - 0.5 * LOG_2PI - log(mu_scale);
-    double lp_tau = -LOG_PI - log(tau_scale) - log1p((dt / tau_scale) * (dt / tau_scale)) + LOG_2 + (double)lt;
-    double total = lp + lp_mu + lp_tau - (double)J * LOG_2PI;  // two N(.) normalisers per group
-    PE[c] = -total;
-    g[0] = (float)(dmu / (mu_scale * mu_scale) - sw);
-    g[1] = (float)(2.0 * dt * dt / (tau_scale * tau_scale + dt * dt) - 1.0 - dt * swe);
-  }
+  hier_nc_potential_warp(Q + (size_t)c * ld, G + (size_t)c * ld, PE + c, J, y + j0, sg + j0, mu_scale, tau_scale,
+                         lane);
 }
 
 // ============================================================ logistic regression (FP32 SIMT)

@@ -66,7 +66,9 @@ class HMC(MCMCKernel):
     """Hamiltonian Monte Carlo with fixed trajectory length (numpyro/infer/hmc.py:541-822).
 
     Extra keyword-only arguments beyond numpyro's:
-      engine: "fused" (per-chain trees, no lock-step) or "plain" (lock-step, numpyro vmap semantics)
+      engine: "fused" (per-chain trees, no lock-step; one persistent launch for the hierarchical
+              family), "ticks" (per-chain trees, one launch per leapfrog step) or "plain"
+              (lock-step, numpyro vmap semantics)
       precision: "fp32" or "bf16x3" (tensor-core logistic potential)
       num_chains: chains to run when ``init`` gets a single key
     """
@@ -94,8 +96,8 @@ class HMC(MCMCKernel):
                 raise ValueError("At least one of `num_steps` or `trajectory_length` must be specified.")
             if adapt_step_size and num_steps is not None and trajectory_length is not None:
                 warnings.warn("If both `num_steps` and `trajectory_length` are specified step size can't be adapted")
-        if engine not in ("fused", "plain"):
-            raise ValueError("engine must be 'fused' or 'plain'")
+        if engine not in ("fused", "plain", "ticks"):
+            raise ValueError("engine must be 'fused', 'plain' or 'ticks'")
         if precision not in ("fp32", "bf16x3"):
             raise ValueError("precision must be 'fp32' or 'bf16x3'")
         self._model = model
@@ -150,7 +152,7 @@ class HMC(MCMCKernel):
         m = self._model
         cfg.chains_per_model = num_chains // getattr(m, "num_models", 1) if hasattr(m, "num_models") else 0
         cfg.algo = _lib.ALGO_NUTS if self._algo == "NUTS" else _lib.ALGO_HMC
-        cfg.engine = _lib.ENGINE_FUSED if self._engine == "fused" else _lib.ENGINE_PLAIN
+        cfg.engine = {"fused": _lib.ENGINE_FUSED, "plain": _lib.ENGINE_PLAIN, "ticks": _lib.ENGINE_TICKS}[self._engine]
         cfg.precision = _lib.PREC_BF16X3 if self._precision == "bf16x3" else _lib.PREC_FP32
         mtd = self._max_tree_depth
         if isinstance(mtd, tuple):

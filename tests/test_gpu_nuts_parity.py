@@ -85,17 +85,28 @@ def test_single_transition_parity(engine):
 
 
 @pytest.mark.gpu
-def test_fused_and_plain_engines_are_bit_identical():
-    model, _ = _hier()
+@pytest.mark.parametrize("uneven", [False, True])
+def test_persistent_tick_and_plain_engines_are_bit_identical(uneven):
+    """The persistent launch (fused), the launch-per-leapfrog tick engine and the lock-step
+    plain engine take identical decisions on identical bits: draws, tree sizes and adapted
+    step sizes agree bit for bit."""
+    if uneven:
+        model = models.HierarchicalNormal(datasets=datasets.uneven_hierarchical(seed=1, num_models=9, jmin=3,
+                                                                                 jmax=40))
+        C = 36
+    else:
+        model, _ = _hier()
+        C = 32
     res = {}
-    for engine in ["fused", "plain"]:
-        k = NUTS(model, num_chains=32, engine=engine)
+    for engine in ["fused", "ticks", "plain"]:
+        k = NUTS(model, num_chains=C, engine=engine)
         st = k.init(SEED, 100)
         out = k.run_device(st, 150, collect_start=0, collect=("z", "num_steps"))
         res[engine] = (out["z"].cpu().numpy(), out["num_steps"].cpu().numpy(), st.adapt_state.step_size.cpu().numpy())
         k.close()
-    for a, b in zip(res["fused"], res["plain"]):
+    for a, b, c in zip(res["fused"], res["ticks"], res["plain"]):
         np.testing.assert_array_equal(a, b)
+        np.testing.assert_array_equal(a, c)
 
 
 @pytest.mark.gpu
