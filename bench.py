@@ -49,7 +49,7 @@ def parse():
                    help="potential: time only the dominant kernel (U and dU for every chain)")
     p.add_argument("--reps", type=int, default=20)
     p.add_argument("--workload", default="logreg",
-                   choices=["logreg", "eight_schools", "uneven_hier", "horseshoe", "sv"],
+                   choices=["logreg", "eight_schools", "uneven_hier", "horseshoe", "sv", "sv_nc"],
                    help="non-default workloads: a full warmup+sampling run of that model family")
     p.add_argument("--samples", type=int, default=None, help="sampling iterations of a --workload run")
     return p.parse_args()
@@ -78,8 +78,9 @@ def run_workload(args):
         shape = "N=2000, P=1000 (D=2002), 256 chains"
     else:
         r, _ = datasets.sv_returns(seed=0)
-        model, C, W, S = models.StochasticVolatility(r), 256, 500, 500
-        shape = "T=4096 (D=4098), 256 chains"
+        nc = w == "sv_nc"
+        model, C, W, S = models.StochasticVolatility(r, noncentered=nc), 256, 1000, 1000
+        shape = "T=4096 (D=4098), 256 chains, %s walk" % ("non-centred" if nc else "centred")
     if args.num_warmup != 500:
         W = args.num_warmup
     if args.samples:
@@ -97,8 +98,22 @@ def run_workload(args):
     torch.cuda.synchronize()
     warm_s, samp_s = ev[0].elapsed_time(ev[1]) / 1e3, ev[1].elapsed_time(ev[2]) / 1e3
     ticks = k.stats()["ticks"] - t_ticks
-    z = out["z"].cpu().numpy()
     ns = out["num_steps"].cpu().numpy()
+    if w in ("sv", "sv_nc"):
+        # every 16th step of the walk plus nu and s keeps the host-side ranking to ~260 coordinates;
+        # the non-centred run adds the derived walk h = s * cumsum(h_base) at the same steps
+        zd = out["z"]
+        T = zd.shape[-1] - 2
+        idx = torch.tensor(list(range(0, T, 16)) + [T, T + 1], device=zd.device)
+        parts = [zd.index_select(2, idx)]
+        if w == "sv_nc":
+            h = torch.exp(zd[..., T + 1:].double()) * torch.cumsum(zd[..., :T].double(), dim=-1)
+            parts.append(h.index_select(2, idx[:-2]).float())
+            del h
+        z = torch.cat(parts, dim=2).cpu().numpy()
+        del zd, parts
+    else:
+        z = out["z"].cpu().numpy()
     if w == "uneven_hier":  # ESS per model over its 4 chains, padding excluded
         Dk = np.array([model.chain_latent_dim(4 * m, 4) for m in range(model.num_models)])
         ess, rhat = [], []
@@ -108,6 +123,9 @@ def run_workload(args):
             rhat.append(r)
         ess_min, rhat_max = float(np.min(ess)), float(np.max(rhat))
         ess_note = "min over a strided sample of 64 models of the per-model min bulk-ESS"
+    elif w in ("sv", "sv_nc"):
+        ess_min, rhat_max = min_bulk_ess(z)
+        ess_note = "min over every 16th step of the walk (h, and h_base when non-centred), nu and s"
     else:
         ess_min, rhat_max = min_bulk_ess(z)
         ess_note = "min over latent coordinates"
@@ -217,8 +235,12 @@ def min_bulk_ess(z):
 
     if z.shape[1] < 4:  # split diagnostics need at least 4 draws per chain
         return float("nan"), float("nan")
-    ess = np.array([bulk_effective_sample_size(z[..., d]) for d in range(z.shape[-1])])
-    rhat = np.array([split_gelman_rubin(z[..., d]) for d in range(z.shape[-1])])
+    ess, rhat = [], []
+    for d0 in range(0, z.shape[-1], 64):  # blocks of coordinates, vectorised over each block
+        blk = np.asarray(z[..., d0:d0 + 64], np.float64)
+        ess.append(np.atleast_1d(bulk_effective_sample_size(blk)))
+        rhat.append(np.atleast_1d(split_gelman_rubin(blk)))
+    ess, rhat = np.concatenate(ess), np.concatenate(rhat)
     return float(ess.min()), float(np.max(rhat))
 
 

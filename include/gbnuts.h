@@ -49,13 +49,17 @@ extern "C" {
 #define GBN_FAMILY_LOGREG 2    /* Bernoulli-logit GLM, Normal(0,1) prior          */
 #define GBN_FAMILY_HORSESHOE 3 /* Gaussian GLM, horseshoe prior                   */
 #define GBN_FAMILY_SV 4        /* Gaussian random walk + StudentT volatility      */
+/* GBN_FAMILY_SV hyper: [0] s rate (Exponential), [1] nu rate (Exponential), [2] = 1 selects the
+ * non-centred walk h = s * cumsum(h_base), h_base ~ Normal(0, 1)^T (0: centred, as numpyro's
+ * GaussianRandomWalk site). */
 
 /* engines */
 #define GBN_ENGINE_FUSED 0 /* per-chain trees, no lock-step, fused/tensor-core potentials */
 #define GBN_ENGINE_PLAIN 1 /* lock-step masked trees (numpyro vmap semantics), FP32 CUDA-core potentials */
 #define GBN_ENGINE_TICKS 2 /* per-chain trees on the launch-per-leapfrog tick engine (no persistent kernel) */
-/* GBN_ENGINE_FUSED runs the hierarchical family in one persistent launch (warps pull chains
- * from a device work queue); other families use the tick engine. */
+/* GBN_ENGINE_FUSED runs the hierarchical family (a warp per chain) and the stochastic-volatility
+ * family (a CTA per chain) in one persistent launch that pulls chains from a device work queue;
+ * other families use the tick engine. */
 
 /* algorithms */
 #define GBN_ALGO_NUTS 0

@@ -34,6 +34,7 @@ struct gbn_handle_s {
   int32_t* err_word = nullptr;
   int32_t* window_end = nullptr;
   int persistent = 0;         // run gbn_run through the persistent engine
+  bool cta_per_chain = false; // advance kernel: a CTA (not a warp) per chain
   int32_t* order = nullptr;   // persistent engine: chain queue order
   int num_windows = 0;
   int num_warmup = 0;
@@ -281,9 +282,13 @@ int gbn_create(gbn_handle* out, const gbn_model_desc* md, const gbn_config* cfg)
     if (ce == cudaSuccess)
       ce = cudaMemcpy(e.chain_dim, chain_dim.data(), sizeof(int32_t) * C, cudaMemcpyHostToDevice);
   }
-  // persistent engine (hierarchical family, non-lock-step): chain queue ordered longest first
-  h->persistent = (m.family == GBN_FAMILY_HIER_NC && cfg->engine == GBN_ENGINE_FUSED);
-  if (ce == cudaSuccess && h->persistent) {
+  // persistent engines (hierarchical and stochastic-volatility families, non-lock-step);
+  // the hierarchical queue is ordered longest chain first
+  h->persistent = ((m.family == GBN_FAMILY_HIER_NC || m.family == GBN_FAMILY_SV) && cfg->engine == GBN_ENGINE_FUSED);
+  // the SV family always runs a CTA per chain, so its tick, plain and persistent engines share
+  // one reduction order and stay bit-identical
+  h->cta_per_chain = (m.family == GBN_FAMILY_SV) || D > 1024;
+  if (ce == cudaSuccess && h->persistent && m.family == GBN_FAMILY_HIER_NC) {
     std::vector<int32_t> order(C);
     for (int c = 0; c < C; ++c) order[c] = c;
     if (!chain_dim.empty())
@@ -380,7 +385,7 @@ static int tick_loop(gbn_handle h, cudaStream_t st, int64_t max_ticks) {
   for (;;) {
     int last = 0;
     for (int k = 0; k < batch; ++k) {
-      launch_advance(h->dP, h->C, h->D, parity, st);
+      launch_advance(h->dP, h->C, h->D, h->cta_per_chain, parity, st);
       cudaError_t e = launch_potential(h->m, h->e.Q, h->C, h->e.PE, h->e.G, h->counters + 2 * parity, st);
       if (e != cudaSuccess) return cuda_fail(h, e, "tick launch");
       last = parity;
@@ -522,9 +527,14 @@ int gbn_run(gbn_handle h, void* stream, gbn_state* st, int32_t num_iterations, i
     // one launch: every chain runs all its transitions from the device work queue
     e = cudaMemsetAsync(h->counters + 7, 0, sizeof(int32_t), s);
     if (e != cudaSuccess) return cuda_fail(h, e, "gbn_run: queue");
-    HierView hv{h->m.y, h->m.sigma, h->m.offsets, h->m.chains_per_model, h->m.num_models, h->m.hyper[0],
-                h->m.hyper[1]};
-    launch_persistent_hier(h->dP, hv, h->counters + 7, h->order, h->C, s);
+    if (h->m.family == GBN_FAMILY_SV) {
+      SvView sv{h->m.y, (int)h->m.n, h->m.hyper[2] != 0.0, h->m.hyper[0], h->m.hyper[1]};
+      launch_persistent_sv(h->dP, sv, h->counters + 7, h->C, s);
+    } else {
+      HierView hv{h->m.y, h->m.sigma, h->m.offsets, h->m.chains_per_model, h->m.num_models, h->m.hyper[0],
+                  h->m.hyper[1]};
+      launch_persistent_hier(h->dP, hv, h->counters + 7, h->order, h->C, s);
+    }
     e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) return cuda_fail(h, e, "gbn_run: persistent engine");

@@ -1,7 +1,8 @@
 // hier_potential.cuh -- warp-level potential + adjoint of the non-centred
 // hierarchical normal model, shared by the tick-engine kernel
 // (potentials_simt.cu) and the persistent engine (nuts_engine.cu) so both
-// produce bit-identical gradients.
+// produce bit-identical gradients.  z and g carry no __restrict__: the persistent
+// engine writes z in the same launch, so its loads must not take the read-only path.
 //
 //   mu ~ Normal(0, mu_scale); tau ~ HalfCauchy(tau_scale) (Exp transform, log-det = log tau);
 //   theta_base_j ~ Normal(0, 1); theta_j = mu + tau * theta_base_j  (numpyro/infer/reparam.py:154-191)
@@ -14,7 +15,7 @@
 
 namespace gbn {
 
-__device__ __forceinline__ void hier_nc_potential_warp(const float* __restrict__ z, float* __restrict__ g,
+__device__ __forceinline__ void hier_nc_potential_warp(const float* z, float* g,
                                                        double* __restrict__ pe_out, int J,
                                                        const float* __restrict__ y, const float* __restrict__ sg,
                                                        double mu_scale, double tau_scale, int lane) {
@@ -23,18 +24,20 @@ __device__ __forceinline__ void hier_nc_potential_warp(const float* __restrict__
   constexpr double LOG_2 = 0.6931471805599453;
   const float mu = z[0], lt = z[1];
   const float tau = expf(lt);
-  double lp = 0.0, sw = 0.0, swe = 0.0;
+  // per-lane partial sums in FP32 (at most 8 terms for J <= 256), summed across the warp in FP64
+  float lpf = 0.0f, swf = 0.0f, swef = 0.0f;
   for (int j = lane; j < J; j += 32) {
     const float eta = z[2 + j];
     const float yy = y[j], s = sg[j];
     const float th = fmaf(tau, eta, mu);
     const float r = (yy - th) / s;
-    lp += (double)(-0.5f * eta * eta - 0.5f * r * r - logf(s));
+    lpf += -0.5f * eta * eta - 0.5f * r * r - logf(s);
     const float w = r / s;
-    sw += (double)w;
-    swe += (double)(w * eta);
+    swf += w;
+    swef = fmaf(w, eta, swef);
     g[2 + j] = eta - tau * w;
   }
+  double lp = lpf, sw = swf, swe = swef;
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
     lp += __shfl_xor_sync(0xffffffffu, lp, o);

@@ -42,10 +42,20 @@ struct HierView {
   double mu_scale, tau_scale;
 };
 
+// device view of the stochastic-volatility data (persistent engine)
+struct SvView {
+  const float* ret;
+  int T;
+  int noncentred;
+  double s_rate, nu_rate;
+};
+
 // nuts_engine.cu
-void launch_advance(const AdvParams* dP, int C, int D, int parity, cudaStream_t st);
+// a CTA per chain when cta_per_chain or D > 1024, else a warp per chain
+void launch_advance(const AdvParams* dP, int C, int D, bool cta_per_chain, int parity, cudaStream_t st);
 void launch_persistent_hier(const AdvParams* dP, const HierView& hv, int32_t* queue_head, const int32_t* order,
                             int C, cudaStream_t st);
+void launch_persistent_sv(const AdvParams* dP, const SvView& sv, int32_t* queue_head, int C, cudaStream_t st);
 void launch_init_uniform(const AdvParams* dP, int C, int D, int attempt, const int32_t* flag, cudaStream_t st);
 void launch_check_valid(const AdvParams* dP, int C, int32_t* flag, int32_t* count, cudaStream_t st);
 void launch_init_state(const AdvParams* dP, int C, int D, const float* inv_mass_init, float init_step,

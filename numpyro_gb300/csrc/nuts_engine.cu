@@ -27,6 +27,7 @@
 #include "common.cuh"
 #include "hier_potential.cuh"
 #include "internal.h"
+#include "sv_potential.cuh"
 
 namespace gbn {
 
@@ -47,28 +48,33 @@ struct Chain {
   __device__ __forceinline__ float* V(float* base) const { return base + row(); }
   __device__ __forceinline__ float* CK(float* base, int k) const { return base + ((size_t)c * P.maxd + k) * ld; }
 
+  // Per-element products and each thread's partial sums are FP32 (numpyro's dtype); the
+  // partials are summed across the group in FP64.  GB300 issues FP64 at a small fraction of
+  // the FP32 rate, so per-element FP64 would dominate leaves of large-D chains.
   // 0.5 * r . (M^-1 r)
   __device__ double kinetic(const float* r) {
     const float* mi = V(P.s.inverse_mass_matrix);
-    double acc = 0.0;
-    for (int d = g.tid; d < D; d += NT) acc += (double)mi[d] * (double)r[d] * (double)r[d];
-    return 0.5 * g.sum(acc, red);
+    float acc = 0.0f;
+    for (int d = g.tid; d < D; d += NT) acc = fmaf(mi[d] * r[d], r[d], acc);
+    return 0.5 * g.sum((double)acc, red);
   }
 
-  // _is_turning: v_l . (rs - (r_l + r_r)/2) <= 0 or v_r . (...) <= 0, with v = M^-1 r
+  // _is_turning: v_l . (rs - (r_l + r_r)/2) <= 0 or v_r . (...) <= 0, with v = M^-1 r;
+  // the subtree sum rs - rs_minus + rs_plus of _is_iterative_turning when rs_minus is given
   __device__ bool is_turning(const float* rl, const float* rr, const float* rs, const float* rs_minus,
                              const float* rs_plus) {
     const float* mi = V(P.s.inverse_mass_matrix);
-    double2 acc = make_double2(0.0, 0.0);
+    float ax = 0.0f, ay = 0.0f;
     for (int d = g.tid; d < D; d += NT) {
-      double s = (double)rs[d];
-      if (rs_minus) s = s - (double)rs_minus[d] + (double)rs_plus[d];
-      double a = (double)rl[d], b = (double)rr[d];
-      s -= 0.5 * (a + b);
-      acc.x += (double)mi[d] * a * s;
-      acc.y += (double)mi[d] * b * s;
+      float s = rs[d];
+      if (rs_minus) s = (s - rs_minus[d]) + rs_plus[d];
+      const float a = rl[d], b = rr[d];
+      s -= 0.5f * (a + b);
+      const float m = mi[d];
+      ax = fmaf(m * a, s, ax);
+      ay = fmaf(m * b, s, ay);
     }
-    double2 t = g.sum2(acc, red);
+    double2 t = g.sum2(make_double2((double)ax, (double)ay), red);
     return (t.x <= 0.0) || (t.y <= 0.0);
   }
 
@@ -117,20 +123,20 @@ struct Chain {
     float *zl = V(P.e.z_l), *zr = V(P.e.z_r), *zp = V(P.e.z_p);
     float *rl = V(P.e.r_l), *rr = V(P.e.r_r), *rs = V(P.e.rsum);
     float *gl = V(P.e.g_l), *grr = V(P.e.g_r), *gp = V(P.e.g_p);
-    double kin = 0.0;
+    float kin = 0.0f;
     const float* mi = V(P.s.inverse_mass_matrix);
     for (int d = g.tid; d < D; d += NT) {
       float r = ms[d] * normal_at(P.seed, chain_id, n, P_MOMENTUM, d, 0);
-      kin += (double)mi[d] * (double)r * (double)r;
+      kin = fmaf(mi[d] * r, r, kin);
       float zz = z[d], gg = gz[d];
       zl[d] = zz; zr[d] = zz; zp[d] = zz;
       gl[d] = gg; grr[d] = gg; gp[d] = gg;
       rl[d] = r; rr[d] = r; rs[d] = r;
     }
-    kin = 0.5 * g.sum(kin, red);
+    const double kin0 = 0.5 * g.sum((double)kin, red);
     int i = P.s.i[c];
     double pe = P.s.potential_energy[c];
-    ctl.energy0 = pe + kin;
+    ctl.energy0 = pe + kin0;
     ctl.step = P.s.step_size[c];
     ctl.depth = 0;
     ctl.tree_w = 0.0;
@@ -275,29 +281,37 @@ struct Chain {
   // returns true if a heuristic step-size search was started (pending)
   __device__ bool adapt(int t, double accept_prob) {
     double* ss = P.s.ss_state + 5 * (size_t)c;
+    // Every thread of the group reads the chain's adaptation scalars before thread 0 updates
+    // them (with a CTA per chain, warps run apart and would otherwise see a mix of old and
+    // new values and take different branches).
     float step = P.s.step_size[c];
+    double x_t = ss[0], x_avg = ss[1], g_avg = ss[2], tt = ss[3];
+    const double prox = ss[4];
+    int widx = P.s.window_idx[c];
+    int nn = P.s.mm_n[c];
+    g.sync();
     if (P.adapt_step) {  // dual_averaging.update_fn, t0=10, kappa=0.75, gamma=0.05
       double g_ = (double)P.target_accept - accept_prob;
-      double x_t = ss[0], x_avg = ss[1], g_avg = ss[2], tt = ss[3], prox = ss[4];
       tt += 1.0;
       g_avg = (1.0 - 1.0 / (tt + 10.0)) * g_avg + g_ / (tt + 10.0);
       x_t = prox - sqrt(tt) / 0.05 * g_avg;
       double wt = pow(tt, -0.75);
       x_avg = (1.0 - wt) * x_avg + wt * x_t;
-      ss[0] = x_t; ss[1] = x_avg; ss[2] = g_avg; ss[3] = tt;
+      if (g.tid == 0) {
+        ss[0] = x_t; ss[1] = x_avg; ss[2] = g_avg; ss[3] = tt;
+      }
       double s = (t == P.num_warmup - 1) ? exp(x_avg) : exp(x_t);
       float sf = (float)s;
       if (!(sf >= FLT32_TINY)) sf = FLT32_TINY;  // also maps NaN to tiny
       if (sf > FLT32_MAX) sf = FLT32_MAX;
       step = sf;
     }
-    int widx = P.s.window_idx[c];
     bool middle = (0 < widx) && (widx < P.num_windows - 1);
     const float* z = V(P.s.z);
     double* mean = P.s.mm_mean + row();
     double* m2 = P.s.mm_m2 + row();
     if (P.adapt_mass && middle) {  // welford update_fn
-      int nn = P.s.mm_n[c] + 1;
+      nn += 1;
       for (int d = g.tid; d < D; d += NT) {
         double x = (double)z[d];
         double dpre = x - mean[d];
@@ -312,8 +326,7 @@ struct Chain {
     if (g.tid == 0) P.s.window_idx[c] = widx;
     bool started = false;
     if (at_end && middle) {
-      if (P.adapt_mass) {  // welford final_fn + Stan regularisation
-        int nn = P.s.mm_n[c];
+      if (P.adapt_mass) {  // welford final_fn + Stan regularisation (nn counts this draw)
         float* inv = V(P.s.inverse_mass_matrix);
         float* sq = V(P.s.mass_matrix_sqrt);
         float* sqi = V(P.s.mass_matrix_sqrt_inv);
@@ -336,7 +349,7 @@ struct Chain {
           g.sync();
           heur_begin(HC_WINDOW, (uint32_t)t);
           started = true;
-        } else {
+        } else if (g.tid == 0) {
           ss[0] = 0.0; ss[1] = 0.0; ss[2] = 0.0; ss[3] = 0.0;
           ss[4] = log(10.0) + log((double)step);
         }
@@ -369,17 +382,17 @@ struct Chain {
     float* r0 = V(P.e.r_l);
     float* rh = V(P.e.r_r);
     float* q = V(P.e.Q);
-    double kin = 0.0;
+    float kin = 0.0f;
     for (int d = g.tid; d < D; d += NT) {
       float r = mi[d] * normal_at(P.seed, chain_id, (uint32_t)ctl.hmc_total, P_HEURISTIC, d,
                                   (uint32_t)ctl.heur_trial);
-      kin += (double)mi[d] * (double)r * (double)r;
+      kin = fmaf(mi[d] * r, r, kin);
       r0[d] = r;
       float h = r - 0.5f * eps * gz[d];
       rh[d] = h;
       q[d] = z[d] + eps * (mi[d] * h);
     }
-    ctl.heur_e0 = P.s.potential_energy[c] + 0.5 * g.sum(kin, red);
+    ctl.heur_e0 = P.s.potential_energy[c] + 0.5 * g.sum((double)kin, red);
     ctl.phase = PH_HEUR;
   }
   // returns true when the search is over (step size in ctl.heur_step)
@@ -388,12 +401,12 @@ struct Chain {
     const float* mi = V(P.s.inverse_mass_matrix);
     const float* G = V(P.e.G);
     const float* rh = V(P.e.r_r);
-    double kin = 0.0;
+    float kin = 0.0f;
     for (int d = g.tid; d < D; d += NT) {
       float rn = rh[d] - 0.5f * eps * G[d];
-      kin += (double)mi[d] * (double)rn * (double)rn;
+      kin = fmaf(mi[d] * rn, rn, kin);
     }
-    double e_new = P.e.PE[c] + 0.5 * g.sum(kin, red);
+    double e_new = P.e.PE[c] + 0.5 * g.sum((double)kin, red);
     double dE = e_new - ctl.heur_e0;
     int dir_new = (log(0.8) < -dE) ? 1 : -1;
     ctl.heur_last = ctl.heur_dir;
@@ -432,8 +445,8 @@ struct Chain {
         gz[d] = gnew[d];
       }
     }
+    const int i = P.s.i[c];  // read by every thread before thread 0 advances it
     g.sync();
-    int i = P.s.i[c];
     int j = ctl.iters_done;
     if (g.tid == 0) {
       P.s.potential_energy[c] = pe_new;
@@ -483,7 +496,10 @@ struct Chain {
   __device__ bool may_start() {
     if (ctl.iters_left <= 0) return false;
     if (!P.lockstep || ctl.iters_done == 0) return true;
-    return *((volatile int32_t*)&P.done_count[ctl.iters_done - 1]) >= P.C;
+    // Other chains raise the count concurrently: thread 0 reads it once and the group sum hands
+    // that one reading to every thread, so all warps of a CTA-per-chain group decide alike.
+    const int cnt = (g.tid == 0) ? *((volatile int32_t*)&P.done_count[ctl.iters_done - 1]) : 0;
+    return g.sum((double)cnt, red) >= (double)P.C;
   }
 
   // ----------------------------------------------------------- driver
@@ -732,6 +748,42 @@ __global__ void __launch_bounds__(256) persistent_hier_kernel(const AdvParams* _
   }
 }
 
+// Stochastic volatility: one CTA per chain (D = T + 2 in the thousands).  Each CTA pops
+// chains from the work queue and runs all their transitions with the CTA-level potential
+// inline, so no leapfrog step costs a kernel launch or a host round trip.  Every thread
+// carries the same ChainCtl (its decisions come from block-wide reductions and the
+// counter-based stream), so the control flow is uniform across the CTA.
+__global__ void __launch_bounds__(256) persistent_sv_kernel(const AdvParams* __restrict__ Pp, SvView sv,
+                                                            int32_t* queue_head) {
+  __shared__ SvSmem<256> sm;
+  __shared__ int next_chain;
+  const AdvParams& P = *Pp;
+  const int tid = threadIdx.x;
+  for (;;) {
+    if (tid == 0) next_chain = atomicAdd(queue_head, 1);
+    __syncthreads();
+    const int c = next_chain;
+    __syncthreads();  // every thread has read next_chain before it is overwritten
+    if (c >= P.C) break;
+    Chain<256> ch{P, Group<256>{tid}, sm.red, c, P.D, P.D, P.e.ctl[c]};
+    ch.run();
+    float* q = P.e.Q + (size_t)c * P.D;
+    float* gr = P.e.G + (size_t)c * P.D;
+    for (;;) {
+      const int ph = ch.ctl.phase;
+      if (!(ph == PH_LEAF || ph == PH_HMC || ph == PH_HEUR)) break;
+      __syncthreads();  // Q written by other threads
+      if (sv.noncentred)
+        sv_nc_potential_block<256>(q, gr, P.e.PE + c, sv.T, sv.ret, sv.s_rate, sv.nu_rate, tid, sm);
+      else
+        sv_potential_block<256>(q, gr, P.e.PE + c, sv.T, sv.ret, sv.s_rate, sv.nu_rate, tid, sm);
+      __syncthreads();  // G and PE written by other threads
+      ch.run();
+    }
+    if (tid == 0) P.e.ctl[c] = ch.ctl;
+  }
+}
+
 // --------------------------------------------------------------------- launchers
 void launch_persistent_hier(const AdvParams* dP, const HierView& hv, int32_t* queue_head, const int32_t* order,
                             int C, cudaStream_t st) {
@@ -746,8 +798,19 @@ void launch_persistent_hier(const AdvParams* dP, const HierView& hv, int32_t* qu
   persistent_hier_kernel<<<blocks, 256, 0, st>>>(dP, hv, queue_head, order);
 }
 
-void launch_advance(const AdvParams* dP, int C, int D, int parity, cudaStream_t st) {
-  if (D <= 1024) {
+void launch_persistent_sv(const AdvParams* dP, const SvView& sv, int32_t* queue_head, int C, cudaStream_t st) {
+  int dev = 0, sms = 0, per_sm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, persistent_sv_kernel, 256, 0);
+  if (per_sm < 1) per_sm = 1;
+  int blocks = sms * per_sm;
+  if (blocks > C) blocks = C;
+  persistent_sv_kernel<<<blocks, 256, 0, st>>>(dP, sv, queue_head);
+}
+
+void launch_advance(const AdvParams* dP, int C, int D, bool cta_per_chain, int parity, cudaStream_t st) {
+  if (!cta_per_chain && D <= 1024) {
     int cpb = 8;
     advance_kernel<32><<<(C + cpb - 1) / cpb, 32 * cpb, 0, st>>>(dP, parity);
   } else {

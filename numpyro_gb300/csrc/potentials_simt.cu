@@ -15,6 +15,7 @@
 #include "common.cuh"
 #include "hier_potential.cuh"
 #include "internal.h"
+#include "sv_potential.cuh"
 
 namespace gbn {
 
@@ -318,53 +319,20 @@ __global__ void __launch_bounds__(256) horseshoe_finish_kernel(const float* __re
 }
 
 // ============================================================ stochastic volatility
-// z = [h(T), log nu, log s]; CTA per point.  Centred GaussianRandomWalk as numpyro.
+// z = [h(T) or h_base(T), log nu, log s]; CTA per point (sv_potential.cuh).
 __global__ void __launch_bounds__(256) sv_kernel(const float* __restrict__ Q, int npts, int ld, int T,
                                                  const float* __restrict__ ret, double s_rate, double nu_rate,
-                                                 double* __restrict__ PE, float* __restrict__ G,
+                                                 int noncentred, double* __restrict__ PE, float* __restrict__ G,
                                                  const int32_t* pending) {
   if (pending && *pending == 0) return;
-  __shared__ double red[16];
-  int c = blockIdx.x, tid = threadIdx.x;
-  Group<256> g{tid};
+  __shared__ SvSmem<256> sm;
+  const int c = blockIdx.x, tid = threadIdx.x;
   const float* z = Q + (size_t)c * ld;
   float* gz = G + (size_t)c * ld;
-  double lnu = z[T], ls = z[T + 1];
-  double nu = exp(lnu), s = exp(ls);
-  float nuf = (float)nu;
-  float inv_s2 = (float)(1.0 / (s * s));
-  double sdd = 0.0, sl1p = 0.0, sfrac = 0.0, sh = 0.0;
-  for (int t = tid; t < T; t += 256) {
-    float h = z[t];
-    float dprev = (t == 0) ? h : h - z[t - 1];
-    float dnext = (t + 1 < T) ? z[t + 1] - h : 0.0f;
-    float rt = ret[t];
-    float yv = rt * expf(-h);
-    float y2 = yv * yv;
-    float q = y2 / nuf;
-    float frac = y2 / (nuf + y2);
-    sdd += (double)(dprev * dprev);
-    sl1p += (double)log1pf(q);
-    sfrac += (double)frac;
-    sh += (double)h;
-    gz[t] = (dprev - dnext) * inv_s2 + 1.0f - (nuf + 1.0f) * frac;
-  }
-  double2 a = g.sum2(make_double2(sdd, sl1p), red);
-  double2 b = g.sum2(make_double2(sfrac, sh), red);
-  if (tid == 0) {
-    double S_dd = a.x, S_l1p = a.y, S_frac = b.x, S_h = b.y;
-    double lp = log(s_rate) - s_rate * s + ls;
-    lp += log(nu_rate) - nu_rate * nu + lnu;
-    lp += -0.5 * S_dd / (s * s) - (double)T * ls - 0.5 * (double)T * LOG_2PI;
-    double zc = 0.5 * lnu + 0.5 * LOG_PI + lgamma(0.5 * nu) - lgamma(0.5 * (nu + 1.0));
-    lp += -0.5 * (nu + 1.0) * S_l1p - S_h - (double)T * zc;
-    PE[c] = -lp;
-    double dnu = -0.5 * S_l1p + 0.5 * (nu + 1.0) / nu * S_frac - 0.5 * (double)T / nu -
-                 0.5 * (double)T * digamma_d(0.5 * nu) + 0.5 * (double)T * digamma_d(0.5 * (nu + 1.0)) - nu_rate;
-    gz[T] = (float)(-(dnu * nu + 1.0));
-    double ds = S_dd / (s * s * s) - (double)T / s - s_rate;
-    gz[T + 1] = (float)(-(ds * s + 1.0));
-  }
+  if (noncentred)
+    sv_nc_potential_block<256>(z, gz, PE + c, T, ret, s_rate, nu_rate, tid, sm);
+  else
+    sv_potential_block<256>(z, gz, PE + c, T, ret, s_rate, nu_rate, tid, sm);
 }
 
 __global__ void scale_rows_kernel(const double* __restrict__ cot, float* __restrict__ G, int npts, int D) {
@@ -468,7 +436,8 @@ cudaError_t launch_potential(ModelDev& m, const float* Q, int npts, double* PE, 
       break;
     }
     case 4:
-      sv_kernel<<<npts, 256, 0, st>>>(Q, npts, ld, (int)m.n, m.y, m.hyper[0], m.hyper[1], PE, G, pending);
+      sv_kernel<<<npts, 256, 0, st>>>(Q, npts, ld, (int)m.n, m.y, m.hyper[0], m.hyper[1], m.hyper[2] != 0.0, PE, G,
+                                      pending);
       break;
     default:
       return cudaErrorInvalidValue;

@@ -22,6 +22,7 @@ Models written as numpyro programs (for reference):
   StochasticVolatility (examples/stochastic_volatility.py:58-66)
       s ~ Exponential(s_rate); nu ~ Exponential(nu_rate)
       h ~ GaussianRandomWalk(scale=s, num_steps=T); r_t ~ StudentT(nu, 0, exp(h_t))
+      noncentered=True: h_base ~ Normal(0, 1)^T; h = s * cumsum(h_base) (deterministic)
 """
 from collections import namedtuple
 import ctypes
@@ -175,12 +176,20 @@ class HorseshoeRegression(Model):
 class StochasticVolatility(Model):
     family = _lib.FAMILY_SV
 
-    def __init__(self, returns, s_rate=10.0, nu_rate=0.1):
+    def __init__(self, returns, s_rate=10.0, nu_rate=0.1, noncentered=False):
         self.returns = np.ascontiguousarray(np.asarray(returns, np.float32).ravel())
         self.s_rate = float(s_rate)
         self.nu_rate = float(nu_rate)
+        self.noncentered = bool(noncentered)
         T = self.returns.size
-        self.sites = (Site("h", T, False), Site("nu", 1, True), Site("s", 1, True))
+        walk = "h_base" if self.noncentered else "h"
+        self.sites = (Site(walk, T, False), Site("nu", 1, True), Site("s", 1, True))
+
+    def postprocess(self, z):
+        out = super().postprocess(z)
+        if self.noncentered:
+            out["h"] = out["s"] * np.cumsum(out["h_base"], axis=-1)
+        return out
 
     def descriptor(self):
         d = _lib.ModelDesc()
@@ -190,6 +199,7 @@ class StochasticVolatility(Model):
         d.y = _fp(self.returns)
         d.hyper[0] = self.s_rate
         d.hyper[1] = self.nu_rate
+        d.hyper[2] = 1.0 if self.noncentered else 0.0
         return d, (self.returns,)
 
 

@@ -184,11 +184,51 @@ def sv_grad(z, r, s_rate=10.0, nu_rate=0.1):
     return g
 
 
+# Non-centred variant: sorted sites h_base, nu, s -> z = [h_base(T), log nu, log s],
+# h = s * cumsum(h_base), h_base ~ Normal(0, 1)^T.
+def sv_nc_potential(z, r, s_rate=10.0, nu_rate=0.1):
+    z = np.asarray(z, np.float64)
+    T = r.shape[0]
+    e, lnu, ls = z[:T], z[T], z[T + 1]
+    nu, s = math.exp(lnu), math.exp(ls)
+    h = s * np.cumsum(e)
+    lp = math.log(s_rate) - s_rate * s + ls
+    lp += math.log(nu_rate) - nu_rate * nu + lnu
+    lp += np.sum(_normal_lp(e, 0.0, 1.0))
+    y = r * np.exp(-h)
+    zt = h + 0.5 * lnu + 0.5 * LOG_PI + gammaln(0.5 * nu) - gammaln(0.5 * (nu + 1.0))
+    lp += np.sum(-0.5 * (nu + 1.0) * np.log1p(y ** 2 / nu) - zt)
+    return -float(lp)
+
+
+def sv_nc_grad(z, r, s_rate=10.0, nu_rate=0.1):
+    z = np.asarray(z, np.float64)
+    T = r.shape[0]
+    e, lnu, ls = z[:T], z[T], z[T + 1]
+    nu, s = math.exp(lnu), math.exp(ls)
+    S = np.cumsum(e)
+    h = s * S
+    y2 = (r * np.exp(-h)) ** 2
+    a = (nu + 1.0) * y2 / (nu + y2) - 1.0          # d log StudentT(r_t | h_t) / d h_t
+    suffix = np.cumsum(a[::-1])[::-1]               # sum_{t >= k} a_t
+    g = np.zeros(T + 2)
+    g[:T] = e - s * suffix
+    dlp_dnu = np.sum(
+        -0.5 * np.log1p(y2 / nu) + 0.5 * (nu + 1.0) * y2 / (nu * (nu + y2))
+        - 0.5 / nu - 0.5 * digamma(0.5 * nu) + 0.5 * digamma(0.5 * (nu + 1.0))
+    )
+    dlp_dnu += -nu_rate
+    g[T] = -(dlp_dnu * nu + 1.0)
+    g[T + 1] = -s * np.sum(a * S) + s_rate * s - 1.0
+    return g
+
+
 FAMILIES = {
     "hier_nc": (hier_nc_potential, hier_nc_grad),
     "logreg": (logreg_potential, logreg_grad),
     "horseshoe": (horseshoe_potential, horseshoe_grad),
     "sv": (sv_potential, sv_grad),
+    "sv_nc": (sv_nc_potential, sv_nc_grad),
 }
 
 

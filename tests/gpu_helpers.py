@@ -19,6 +19,9 @@ def family_cases(small=True):
                 PR.make_potential("horseshoe", Xh.astype(np.float64), yh.astype(np.float64))))
     r, _ = datasets.sv_returns(seed=3, T=300)
     out.append(("sv", models.StochasticVolatility(r), PR.make_potential("sv", r.astype(np.float64))))
+    r2, _ = datasets.sv_returns(seed=4, T=1000)
+    out.append(("sv_nc", models.StochasticVolatility(r2, noncentered=True),
+                PR.make_potential("sv_nc", r2.astype(np.float64))))
     return out
 
 
@@ -31,6 +34,13 @@ def typical_points(name, model, rng, C):
         z[:, :T] = np.log(0.01) + 0.3 * rng.standard_normal((C, T))
         z[:, T] = np.log(8.0) + 0.3 * rng.standard_normal(C)
         z[:, T + 1] = np.log(0.02) + 0.3 * rng.standard_normal(C)
+        return z.astype(np.float32)
+    if name == "sv_nc":
+        T = D - 2
+        z = np.empty((C, D))
+        z[:, :T] = 0.3 * rng.standard_normal((C, T))
+        z[:, T] = np.log(8.0) + 0.3 * rng.standard_normal(C)
+        z[:, T + 1] = np.log(0.05) + 0.3 * rng.standard_normal(C)
         return z.astype(np.float32)
     if name == "logreg":
         return (0.3 * rng.standard_normal((C, D))).astype(np.float32)

@@ -81,6 +81,10 @@ def test_model_layout_sorted_sites():
     assert out["sigma"].item() == 1.0 and out["beta"].shape == (3,)
     sv = models.StochasticVolatility(np.zeros(10))
     assert [s.name for s in sv.sites] == ["h", "nu", "s"] and sv.latent_dim == 12
+    nc = models.StochasticVolatility(np.zeros(10), noncentered=True)
+    assert [s.name for s in nc.sites] == ["h_base", "nu", "s"] and nc.latent_dim == 12
+    z = np.concatenate([np.ones(10), [0.0, np.log(0.5)]])
+    np.testing.assert_allclose(nc.postprocess(z)["h"], 0.5 * np.arange(1, 11))
 
 
 def test_adaptation_schedule_host_matches_oracle():

@@ -85,23 +85,29 @@ def test_single_transition_parity(engine):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("uneven", [False, True])
-def test_persistent_tick_and_plain_engines_are_bit_identical(uneven):
+@pytest.mark.parametrize("case", ["hier", "uneven", "sv", "sv_nc"])
+def test_persistent_tick_and_plain_engines_are_bit_identical(case):
     """The persistent launch (fused), the launch-per-leapfrog tick engine and the lock-step
     plain engine take identical decisions on identical bits: draws, tree sizes and adapted
-    step sizes agree bit for bit."""
-    if uneven:
+    step sizes agree bit for bit.  The hierarchical family runs a warp per chain, the
+    stochastic-volatility family a CTA per chain."""
+    iters = 150
+    if case == "uneven":
         model = models.HierarchicalNormal(datasets=datasets.uneven_hierarchical(seed=1, num_models=9, jmin=3,
                                                                                  jmax=40))
         C = 36
+    elif case in ("sv", "sv_nc"):
+        r, _ = datasets.sv_returns(seed=2, T=300)
+        model = models.StochasticVolatility(r, noncentered=(case == "sv_nc"))
+        C, iters = 8, 60
     else:
         model, _ = _hier()
         C = 32
     res = {}
     for engine in ["fused", "ticks", "plain"]:
-        k = NUTS(model, num_chains=C, engine=engine)
-        st = k.init(SEED, 100)
-        out = k.run_device(st, 150, collect_start=0, collect=("z", "num_steps"))
+        k = NUTS(model, num_chains=C, engine=engine, max_tree_depth=8)
+        st = k.init(SEED, iters // 2)
+        out = k.run_device(st, iters, collect_start=0, collect=("z", "num_steps"))
         res[engine] = (out["z"].cpu().numpy(), out["num_steps"].cpu().numpy(), st.adapt_state.step_size.cpu().numpy())
         k.close()
     for a, b, c in zip(res["fused"], res["ticks"], res["plain"]):
