@@ -241,6 +241,20 @@ int gbn_create(gbn_handle* out, const gbn_model_desc* md, const gbn_config* cfg)
       if (ce == cudaSuccess) ce = dalloc(h, &m.y, md->n);
       if (ce == cudaSuccess) ce = cudaMemcpy(m.x, md->x, sizeof(float) * nx, cudaMemcpyHostToDevice);
       if (ce == cudaSuccess) ce = cudaMemcpy(m.y, md->y, sizeof(float) * md->n, cudaMemcpyHostToDevice);
+      if (ce == cudaSuccess && m.family == GBN_FAMILY_HORSESHOE) {
+        // operand layouts of the horseshoe GEMMs: X^T and X, rows zero-padded to 4 floats
+        const size_t n = (size_t)md->n, p = (size_t)md->p, np4 = (size_t)pad4((int)n), pp4 = (size_t)pad4((int)p);
+        std::vector<float> xt(p * np4, 0.0f), xp(n * pp4, 0.0f);
+        for (size_t r = 0; r < n; ++r)
+          for (size_t k = 0; k < p; ++k) {
+            xt[k * np4 + r] = md->x[r * p + k];
+            xp[r * pp4 + k] = md->x[r * p + k];
+          }
+        ce = dalloc(h, &m.hs_xt, xt.size());
+        if (ce == cudaSuccess) ce = dalloc(h, &m.hs_xp, xp.size());
+        if (ce == cudaSuccess) ce = cudaMemcpy(m.hs_xt, xt.data(), sizeof(float) * xt.size(), cudaMemcpyHostToDevice);
+        if (ce == cudaSuccess) ce = cudaMemcpy(m.hs_xp, xp.data(), sizeof(float) * xp.size(), cudaMemcpyHostToDevice);
+      }
       break;
     }
     case GBN_FAMILY_SV: {

@@ -86,6 +86,41 @@ __device__ __forceinline__ double logaddexp_d(double a, double b) {
 }
 __device__ __forceinline__ double sigmoid_d(double x) { return 1.0 / (1.0 + exp(-x)); }
 
+// Tree weights and energy differences are carried in FP64; the transcendental factors applied
+// to an FP64 difference are evaluated in FP32 (GB300 issues FP64 at a small fraction of the FP32
+// rate and these run on every leaf of every chain).
+// log(e^a + e^b): FP64 maximum plus an FP32 correction log1p(e^-|a-b|) (absolute error < 1e-7).
+__device__ __forceinline__ double logaddexp_mixed(double a, double b) {
+  double m = fmax(a, b);
+  if (m == -INFINITY) return -INFINITY;
+  return m + (double)log1pf(expf(-(float)fabs(a - b)));
+}
+// min(1, e^x) and 1 / (1 + e^-x) of an FP64 argument, in FP32
+__device__ __forceinline__ float exp_min1_f(double x) { return fminf(expf((float)x), 1.0f); }
+__device__ __forceinline__ float sigmoid_f(double x) { return 1.0f / (1.0f + expf(-(float)x)); }
+
+// ---------------------------------------------------------------- float-float sums
+// An unevaluated pair hi + lo of FP32 numbers (Dekker 1971).  ff_add is Knuth's exact two-sum
+// of the leading parts plus the trailing parts, renormalised; it is commutative bit for bit, so a
+// butterfly reduction leaves every lane with the same pair.  Group sums use it instead of FP64
+// adds: about 2^-44 relative error, no FP64 instruction.
+struct FF {
+  float hi, lo;
+};
+__device__ __forceinline__ FF ff_add(FF a, FF b) {
+  const float s = a.hi + b.hi;
+  const float bp = s - a.hi;
+  float e = (a.hi - (s - bp)) + (b.hi - bp);
+  e += a.lo + b.lo;
+  const float hi = s + e;
+  return FF{hi, e - (hi - s)};
+}
+__device__ __forceinline__ FF ff_from(float x) { return FF{x, 0.0f}; }
+__device__ __forceinline__ double ff_value(FF a) { return (double)a.hi + (double)a.lo; }
+__device__ __forceinline__ FF ff_shfl_xor(FF v, int o) {
+  return FF{__shfl_xor_sync(0xffffffffu, v.hi, o), __shfl_xor_sync(0xffffffffu, v.lo, o)};
+}
+
 // digamma by upward recurrence to x >= 6 and the asymptotic series
 // psi(x) ~ ln x - 1/(2x) - sum_k B_2k / (2k x^2k) (Abramowitz & Stegun 6.3.18).
 __host__ __device__ inline double digamma_d(double x) {
@@ -97,6 +132,26 @@ __host__ __device__ inline double digamma_d(double x) {
   double r = 1.0 / x, r2 = r * r;
   double series = r2 * (1.0 / 12 - r2 * (1.0 / 120 - r2 * (1.0 / 252 - r2 * (1.0 / 240 - r2 * (1.0 / 132)))));
   return acc + log(x) - 0.5 * r - series;
+}
+
+// Compensated FP32 accumulator (two-sum; the error term is carried separately).
+struct Comp32 {
+  float s, c;
+  __device__ __forceinline__ void add(float x) {
+    float t = s + x;
+    float bp = t - s;
+    c += (s - (t - bp)) + (x - bp);
+    s = t;
+  }
+  __device__ __forceinline__ float value() const { return s + c; }
+};
+
+// Long per-thread sums are accumulated in compensated FP32 and the shares summed across the
+// group as float-float pairs, converted to FP64 for the scalar terms.
+__device__ __forceinline__ double comp_total(const Comp32& a) { return (double)a.s + (double)a.c; }
+__device__ __forceinline__ FF comp_ff(const Comp32& a) {  // renormalised pair (|c| << |s|)
+  const float hi = a.s + a.c;
+  return FF{hi, a.c - (hi - a.s)};
 }
 
 // ---------------------------------------------------------------- engine
@@ -210,6 +265,18 @@ template <>
 struct Group<32> {  // one warp per chain
   int tid;
   __device__ __forceinline__ void sync() const { __syncwarp(); }
+  __device__ __forceinline__ FF sumff(FF v, double*) const {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = ff_add(v, ff_shfl_xor(v, o));
+    return v;
+  }
+  __device__ __forceinline__ void sum2ff(FF& a, FF& b, double*) const {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      a = ff_add(a, ff_shfl_xor(a, o));
+      b = ff_add(b, ff_shfl_xor(b, o));
+    }
+  }
   __device__ __forceinline__ double sum(double v, double*) const {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
@@ -234,6 +301,41 @@ template <>
 struct Group<256> {  // one CTA of 256 threads per chain; red must hold 16 doubles
   int tid;
   __device__ __forceinline__ void sync() const { __syncthreads(); }
+  // warp butterflies, then every thread folds the 8 warp pairs in the same order
+  __device__ __forceinline__ FF sumff(FF v, double* red) const {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = ff_add(v, ff_shfl_xor(v, o));
+    float2* r = reinterpret_cast<float2*>(red);
+    __syncthreads();
+    if ((tid & 31) == 0) r[tid >> 5] = make_float2(v.hi, v.lo);
+    __syncthreads();
+    FF t{r[0].x, r[0].y};
+#pragma unroll
+    for (int w = 1; w < 8; ++w) t = ff_add(t, FF{r[w].x, r[w].y});
+    return t;
+  }
+  __device__ __forceinline__ void sum2ff(FF& a, FF& b, double* red) const {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      a = ff_add(a, ff_shfl_xor(a, o));
+      b = ff_add(b, ff_shfl_xor(b, o));
+    }
+    float2* r = reinterpret_cast<float2*>(red);
+    __syncthreads();
+    if ((tid & 31) == 0) {
+      r[tid >> 5] = make_float2(a.hi, a.lo);
+      r[8 + (tid >> 5)] = make_float2(b.hi, b.lo);
+    }
+    __syncthreads();
+    FF ta{r[0].x, r[0].y}, tb{r[8].x, r[8].y};
+#pragma unroll
+    for (int w = 1; w < 8; ++w) {
+      ta = ff_add(ta, FF{r[w].x, r[w].y});
+      tb = ff_add(tb, FF{r[8 + w].x, r[8 + w].y});
+    }
+    a = ta;
+    b = tb;
+  }
   __device__ __forceinline__ double sum(double v, double* red) const {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);

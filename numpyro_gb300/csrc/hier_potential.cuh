@@ -13,6 +13,8 @@
 #include <cuda_runtime.h>
 #include <math.h>
 
+#include "common.cuh"
+
 namespace gbn {
 
 __device__ __forceinline__ void hier_nc_potential_warp(const float* z, float* g,
@@ -24,7 +26,8 @@ __device__ __forceinline__ void hier_nc_potential_warp(const float* z, float* g,
   constexpr double LOG_2 = 0.6931471805599453;
   const float mu = z[0], lt = z[1];
   const float tau = expf(lt);
-  // per-lane partial sums in FP32 (at most 8 terms for J <= 256), summed across the warp in FP64
+  // per-lane partial sums in FP32 (at most 8 terms for J <= 256), summed across the warp as
+  // float-float pairs
   float lpf = 0.0f, swf = 0.0f, swef = 0.0f;
   for (int j = lane; j < J; j += 32) {
     const float eta = z[2 + j];
@@ -37,13 +40,14 @@ __device__ __forceinline__ void hier_nc_potential_warp(const float* z, float* g,
     swef = fmaf(w, eta, swef);
     g[2 + j] = eta - tau * w;
   }
-  double lp = lpf, sw = swf, swe = swef;
+  FF flp = ff_from(lpf), fsw = ff_from(swf), fswe = ff_from(swef);
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
-    lp += __shfl_xor_sync(0xffffffffu, lp, o);
-    sw += __shfl_xor_sync(0xffffffffu, sw, o);
-    swe += __shfl_xor_sync(0xffffffffu, swe, o);
+    flp = ff_add(flp, ff_shfl_xor(flp, o));
+    fsw = ff_add(fsw, ff_shfl_xor(fsw, o));
+    fswe = ff_add(fswe, ff_shfl_xor(fswe, o));
   }
+  const double lp = ff_value(flp), sw = ff_value(fsw), swe = ff_value(fswe);
   if (lane == 0) {
     const double dmu = (double)mu, dt = exp((double)lt);
     const double lp_mu = -0.5 * (dmu / mu_scale) * (dmu / mu_scale) - 0.5 * LOG_2PI - log(mu_scale);

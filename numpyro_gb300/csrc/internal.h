@@ -30,6 +30,10 @@ struct ModelDev {
   float* part_gb = nullptr;   // horseshoe split-K partials
   double* part_rr = nullptr;  // horseshoe [row tiles][points]
   void* tc = nullptr;         // tensor-core path state (logreg_tc.cu)
+  // horseshoe: X^T [P][pad4(n)] and X [n][pad4(P)] zero-padded, beta^T scratch [pad4(P)][pad4(points)]
+  float* hs_xt = nullptr;
+  float* hs_xp = nullptr;
+  float* hs_bt = nullptr;
 };
 
 // device view of the hierarchical family's data (persistent engine)
@@ -49,6 +53,8 @@ struct SvView {
   int noncentred;
   double s_rate, nu_rate;
 };
+
+inline int pad4(int v) { return (v + 3) & ~3; }
 
 // nuts_engine.cu
 // a CTA per chain when cta_per_chain or D > 1024, else a warp per chain

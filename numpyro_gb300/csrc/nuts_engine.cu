@@ -49,14 +49,32 @@ struct Chain {
   __device__ __forceinline__ float* CK(float* base, int k) const { return base + ((size_t)c * P.maxd + k) * ld; }
 
   // Per-element products and each thread's partial sums are FP32 (numpyro's dtype); the
-  // partials are summed across the group in FP64.  GB300 issues FP64 at a small fraction of
-  // the FP32 rate, so per-element FP64 would dominate leaves of large-D chains.
+  // partials are summed across the group as float-float pairs and used as FP64.  GB300 issues
+  // FP64 at a small fraction of the FP32 rate, so per-element FP64 (or FP64 reductions run by
+  // every thread of the group) would dominate the leaves of large-D chains.
+  // Element loops are blocked by UB: a thread issues the loads of UB of its elements before any
+  // store, so one memory round trip covers UB elements (stores to one chain buffer and loads
+  // from another could otherwise not be reordered by the compiler).  Each thread only ever
+  // touches its own elements d = tid + k * NT, in increasing d, so results do not depend on UB.
+  static constexpr int UB = 4;
+
   // 0.5 * r . (M^-1 r)
   __device__ double kinetic(const float* r) {
     const float* mi = V(P.s.inverse_mass_matrix);
     float acc = 0.0f;
-    for (int d = g.tid; d < D; d += NT) acc = fmaf(mi[d] * r[d], r[d], acc);
-    return 0.5 * g.sum((double)acc, red);
+    for (int d0 = g.tid; d0 < D; d0 += UB * NT) {
+      float rr[UB], mm[UB];
+#pragma unroll
+      for (int k = 0; k < UB; ++k) {
+        const int d = d0 + k * NT;
+        rr[k] = (d < D) ? r[d] : 0.0f;
+        mm[k] = (d < D) ? mi[d] : 0.0f;
+      }
+#pragma unroll
+      for (int k = 0; k < UB; ++k)
+        if (d0 + k * NT < D) acc = fmaf(mm[k] * rr[k], rr[k], acc);
+    }
+    return 0.5 * ff_value(g.sumff(ff_from(acc), red));
   }
 
   // _is_turning: v_l . (rs - (r_l + r_r)/2) <= 0 or v_r . (...) <= 0, with v = M^-1 r;
@@ -65,21 +83,40 @@ struct Chain {
                              const float* rs_plus) {
     const float* mi = V(P.s.inverse_mass_matrix);
     float ax = 0.0f, ay = 0.0f;
-    for (int d = g.tid; d < D; d += NT) {
-      float s = rs[d];
-      if (rs_minus) s = (s - rs_minus[d]) + rs_plus[d];
-      const float a = rl[d], b = rr[d];
-      s -= 0.5f * (a + b);
-      const float m = mi[d];
-      ax = fmaf(m * a, s, ax);
-      ay = fmaf(m * b, s, ay);
+    for (int d0 = g.tid; d0 < D; d0 += UB * NT) {
+      float sv[UB], av[UB], bv[UB], mv[UB];
+#pragma unroll
+      for (int k = 0; k < UB; ++k) {
+        const int d = d0 + k * NT;
+        const bool in = d < D;
+        sv[k] = in ? rs[d] : 0.0f;
+        if (rs_minus) sv[k] = in ? (sv[k] - rs_minus[d]) + rs_plus[d] : 0.0f;
+        av[k] = in ? rl[d] : 0.0f;
+        bv[k] = in ? rr[d] : 0.0f;
+        mv[k] = in ? mi[d] : 0.0f;
+      }
+#pragma unroll
+      for (int k = 0; k < UB; ++k) {
+        if (d0 + k * NT >= D) continue;
+        const float s = sv[k] - 0.5f * (av[k] + bv[k]);
+        ax = fmaf(mv[k] * av[k], s, ax);
+        ay = fmaf(mv[k] * bv[k], s, ay);
+      }
     }
-    double2 t = g.sum2(make_double2((double)ax, (double)ay), red);
-    return (t.x <= 0.0) || (t.y <= 0.0);
+    FF tx = ff_from(ax), ty = ff_from(ay);
+    g.sum2ff(tx, ty, red);
+    return (ff_value(tx) <= 0.0) || (ff_value(ty) <= 0.0);
   }
 
   __device__ void copy(float* dst, const float* src) {
-    for (int d = g.tid; d < D; d += NT) dst[d] = src[d];
+    for (int d0 = g.tid; d0 < D; d0 += UB * NT) {
+      float v[UB];
+#pragma unroll
+      for (int k = 0; k < UB; ++k) v[k] = (d0 + k * NT < D) ? src[d0 + k * NT] : 0.0f;
+#pragma unroll
+      for (int k = 0; k < UB; ++k)
+        if (d0 + k * NT < D) dst[d0 + k * NT] = v[k];
+    }
   }
 
   // ----------------------------------------------------------- leapfrog halves
@@ -90,12 +127,27 @@ struct Chain {
     const float* gr = V(right ? P.e.g_r : P.e.g_l);
     const float* mi = V(P.s.inverse_mass_matrix);
     float* q = V(P.e.Q);
-    for (int d = g.tid; d < D; d += NT) {
-      float rh = r[d] - 0.5f * eps * gr[d];
-      float zn = z[d] + eps * (mi[d] * rh);
-      r[d] = rh;
-      z[d] = zn;
-      q[d] = zn;
+    for (int d0 = g.tid; d0 < D; d0 += UB * NT) {
+      float zz[UB], rr[UB], gg[UB], mm[UB];
+#pragma unroll
+      for (int k = 0; k < UB; ++k) {
+        const int d = d0 + k * NT;
+        const bool in = d < D;
+        zz[k] = in ? z[d] : 0.0f;
+        rr[k] = in ? r[d] : 0.0f;
+        gg[k] = in ? gr[d] : 0.0f;
+        mm[k] = in ? mi[d] : 0.0f;
+      }
+#pragma unroll
+      for (int k = 0; k < UB; ++k) {
+        const int d = d0 + k * NT;
+        if (d >= D) continue;
+        float rh = rr[k] - 0.5f * eps * gg[k];
+        float zn = zz[k] + eps * (mm[k] * rh);
+        r[d] = rh;
+        z[d] = zn;
+        q[d] = zn;
+      }
     }
   }
   // second half-kick with the new gradient; returns K(r_new)
@@ -103,12 +155,29 @@ struct Chain {
     float* r = V(right ? P.e.r_r : P.e.r_l);
     float* gr = V(right ? P.e.g_r : P.e.g_l);
     const float* G = V(P.e.G);
-    for (int d = g.tid; d < D; d += NT) {
-      float gn = G[d];
-      r[d] = r[d] - 0.5f * eps * gn;
-      gr[d] = gn;
+    const float* mi = V(P.s.inverse_mass_matrix);
+    float acc = 0.0f;  // kinetic energy of the new momentum, as kinetic()
+    for (int d0 = g.tid; d0 < D; d0 += UB * NT) {
+      float gn[UB], rr[UB], mm[UB];
+#pragma unroll
+      for (int k = 0; k < UB; ++k) {
+        const int d = d0 + k * NT;
+        const bool in = d < D;
+        gn[k] = in ? G[d] : 0.0f;
+        rr[k] = in ? r[d] : 0.0f;
+        mm[k] = in ? mi[d] : 0.0f;
+      }
+#pragma unroll
+      for (int k = 0; k < UB; ++k) {
+        const int d = d0 + k * NT;
+        if (d >= D) continue;
+        const float rn = rr[k] - 0.5f * eps * gn[k];
+        r[d] = rn;
+        gr[d] = gn[k];
+        acc = fmaf(mm[k] * rn, rn, acc);
+      }
     }
-    return kinetic(r);
+    return 0.5 * ff_value(g.sumff(ff_from(acc), red));
   }
 
   __device__ float signed_step() const { return ctl.dir ? ctl.step : -ctl.step; }
@@ -125,15 +194,29 @@ struct Chain {
     float *gl = V(P.e.g_l), *grr = V(P.e.g_r), *gp = V(P.e.g_p);
     float kin = 0.0f;
     const float* mi = V(P.s.inverse_mass_matrix);
-    for (int d = g.tid; d < D; d += NT) {
-      float r = ms[d] * normal_at(P.seed, chain_id, n, P_MOMENTUM, d, 0);
-      kin = fmaf(mi[d] * r, r, kin);
-      float zz = z[d], gg = gz[d];
-      zl[d] = zz; zr[d] = zz; zp[d] = zz;
-      gl[d] = gg; grr[d] = gg; gp[d] = gg;
-      rl[d] = r; rr[d] = r; rs[d] = r;
+    for (int d0 = g.tid; d0 < D; d0 += UB * NT) {
+      float msv[UB], miv[UB], zv[UB], gv[UB];
+#pragma unroll
+      for (int k = 0; k < UB; ++k) {
+        const int d = d0 + k * NT;
+        const bool in = d < D;
+        msv[k] = in ? ms[d] : 0.0f;
+        miv[k] = in ? mi[d] : 0.0f;
+        zv[k] = in ? z[d] : 0.0f;
+        gv[k] = in ? gz[d] : 0.0f;
+      }
+#pragma unroll
+      for (int k = 0; k < UB; ++k) {
+        const int d = d0 + k * NT;
+        if (d >= D) continue;
+        float r = msv[k] * normal_at(P.seed, chain_id, n, P_MOMENTUM, d, 0);
+        kin = fmaf(miv[k] * r, r, kin);
+        zl[d] = zv[k]; zr[d] = zv[k]; zp[d] = zv[k];
+        gl[d] = gv[k]; grr[d] = gv[k]; gp[d] = gv[k];
+        rl[d] = r; rr[d] = r; rs[d] = r;
+      }
     }
-    const double kin0 = 0.5 * g.sum((double)kin, red);
+    const double kin0 = 0.5 * ff_value(g.sumff(ff_from(kin), red));
     int i = P.s.i[c];
     double pe = P.s.potential_energy[c];
     ctl.energy0 = pe + kin0;
@@ -166,7 +249,7 @@ struct Chain {
     uint32_t n = P.s.rng_key[2 * c + 1];
     uint32_t chain_id = P.s.rng_key[2 * c];
     uint4 w = draw(P.seed, chain_id, n, P_DOUBLING, (uint32_t)ctl.depth, 0);
-    ctl.dir = u01d(w.x) < 0.5 ? 1 : 0;
+    ctl.dir = u01f(w.x) < 0.5f ? 1 : 0;
     ctl.sub_num = 0;
     ctl.sub_div = 0;
     ctl.sub_turning = 0;
@@ -186,7 +269,7 @@ struct Chain {
     if (isnan(dE)) dE = INFINITY;
     double w = -dE;
     int div = dE > P.max_dE;
-    double acc = fmin(exp(-dE), 1.0);
+    double acc = (double)exp_min1_f(-dE);
     const float* zf = V(right ? P.e.z_r : P.e.z_l);
     const float* rf = V(right ? P.e.r_r : P.e.r_l);
     const float* gf = V(right ? P.e.g_r : P.e.g_l);
@@ -195,31 +278,60 @@ struct Chain {
     float* rss = V(P.e.rsum_sub);
     int leaf_idx = ctl.sub_num;
     if (leaf_idx == 0) {
-      for (int d = g.tid; d < D; d += NT) {
-        zsp[d] = zf[d];
-        gsp[d] = gf[d];
-        rss[d] = rf[d];
+      for (int d0 = g.tid; d0 < D; d0 += UB * NT) {
+        float zv[UB], gv[UB], rv[UB];
+#pragma unroll
+        for (int k = 0; k < UB; ++k) {
+          const int d = d0 + k * NT;
+          const bool in = d < D;
+          zv[k] = in ? zf[d] : 0.0f;
+          gv[k] = in ? gf[d] : 0.0f;
+          rv[k] = in ? rf[d] : 0.0f;
+        }
+#pragma unroll
+        for (int k = 0; k < UB; ++k) {
+          const int d = d0 + k * NT;
+          if (d >= D) continue;
+          zsp[d] = zv[k];
+          gsp[d] = gv[k];
+          rss[d] = rv[k];
+        }
       }
       ctl.sub_w = w;
       ctl.pe_sp = pe;
       ctl.energy_sp = e_new;
       ctl.sub_acc = acc;
     } else {
-      double p = sigmoid_d(w - ctl.sub_w);
+      const float p = sigmoid_f(w - ctl.sub_w);
       uint4 u = draw(P.seed, chain_id, n, P_LEAF, (uint32_t)ctl.depth, (uint32_t)leaf_idx);
-      bool take = u01d(u.x) < p;
-      for (int d = g.tid; d < D; d += NT) {
-        if (take) {
-          zsp[d] = zf[d];
-          gsp[d] = gf[d];
+      bool take = u01f(u.x) < p;
+      for (int d0 = g.tid; d0 < D; d0 += UB * NT) {
+        float zv[UB], gv[UB], rv[UB], sv[UB];
+#pragma unroll
+        for (int k = 0; k < UB; ++k) {
+          const int d = d0 + k * NT;
+          const bool in = d < D;
+          zv[k] = (in && take) ? zf[d] : 0.0f;
+          gv[k] = (in && take) ? gf[d] : 0.0f;
+          rv[k] = in ? rf[d] : 0.0f;
+          sv[k] = in ? rss[d] : 0.0f;
         }
-        rss[d] += rf[d];
+#pragma unroll
+        for (int k = 0; k < UB; ++k) {
+          const int d = d0 + k * NT;
+          if (d >= D) continue;
+          if (take) {
+            zsp[d] = zv[k];
+            gsp[d] = gv[k];
+          }
+          rss[d] = sv[k] + rv[k];
+        }
       }
       if (take) {
         ctl.pe_sp = pe;
         ctl.energy_sp = e_new;
       }
-      ctl.sub_w = logaddexp_d(ctl.sub_w, w);
+      ctl.sub_w = logaddexp_mixed(ctl.sub_w, w);
       ctl.sub_acc += acc;
     }
     ctl.sub_div = div;
@@ -229,12 +341,8 @@ struct Chain {
     int num_sub = __popc((unsigned)((~leaf_idx & (leaf_idx + 1)) - 1));
     int idx_min = idx_max - num_sub + 1;
     if ((leaf_idx & 1) == 0) {
-      float* rck = CK(P.e.r_ck, idx_max);
-      float* sck = CK(P.e.rs_ck, idx_max);
-      for (int d = g.tid; d < D; d += NT) {
-        rck[d] = rf[d];
-        sck[d] = rss[d];
-      }
+      copy(CK(P.e.r_ck, idx_max), rf);
+      copy(CK(P.e.rs_ck, idx_max), rss);
     }
     g.sync();
     bool turning = false;
@@ -251,18 +359,29 @@ struct Chain {
     uint32_t chain_id = P.s.rng_key[2 * c];
     float* rs = V(P.e.rsum);
     const float* rss = V(P.e.rsum_sub);
-    for (int d = g.tid; d < D; d += NT) rs[d] += rss[d];
+    for (int d0 = g.tid; d0 < D; d0 += UB * NT) {
+      float a[UB], b[UB];
+#pragma unroll
+      for (int k = 0; k < UB; ++k) {
+        const int d = d0 + k * NT;
+        a[k] = (d < D) ? rs[d] : 0.0f;
+        b[k] = (d < D) ? rss[d] : 0.0f;
+      }
+#pragma unroll
+      for (int k = 0; k < UB; ++k)
+        if (d0 + k * NT < D) rs[d0 + k * NT] = a[k] + b[k];
+    }
     g.sync();
-    double p;
+    float p;
     if (ctl.sub_turning || ctl.sub_div) {
-      p = 0.0;
+      p = 0.0f;
     } else {
-      p = fmin(exp(ctl.sub_w - ctl.tree_w), 1.0);
+      p = exp_min1_f(ctl.sub_w - ctl.tree_w);
     }
     bool turning = ctl.sub_turning;
     if (!turning) turning = is_turning(V(P.e.r_l), V(P.e.r_r), rs, nullptr, nullptr);
     uint4 u = draw(P.seed, chain_id, n, P_DOUBLING, (uint32_t)ctl.depth, 0);
-    bool take = u01d(u.y) < p;
+    bool take = u01f(u.y) < p;
     if (take) {
       copy(V(P.e.z_p), V(P.e.z_sp));
       copy(V(P.e.g_p), V(P.e.g_sp));
@@ -270,7 +389,7 @@ struct Chain {
       ctl.energy_p = ctl.energy_sp;
     }
     ctl.depth += 1;
-    ctl.tree_w = logaddexp_d(ctl.tree_w, ctl.sub_w);
+    ctl.tree_w = logaddexp_mixed(ctl.tree_w, ctl.sub_w);
     ctl.tree_div = ctl.sub_div;
     ctl.tree_acc += ctl.sub_acc;
     ctl.num_prop += ctl.sub_num;
@@ -292,16 +411,18 @@ struct Chain {
     g.sync();
     if (P.adapt_step) {  // dual_averaging.update_fn, t0=10, kappa=0.75, gamma=0.05
       double g_ = (double)P.target_accept - accept_prob;
+      // the state stays FP64; the factors 1/(t+t0), sqrt(t)/gamma and t^-kappa of the integer
+      // count t are formed with one FP64 division and FP32 sqrt/pow (correctly rounded / 1 ulp)
       tt += 1.0;
-      g_avg = (1.0 - 1.0 / (tt + 10.0)) * g_avg + g_ / (tt + 10.0);
-      x_t = prox - sqrt(tt) / 0.05 * g_avg;
-      double wt = pow(tt, -0.75);
+      const double inv_t = 1.0 / (tt + 10.0);
+      g_avg = (1.0 - inv_t) * g_avg + g_ * inv_t;
+      x_t = prox - 20.0 * (double)sqrtf((float)tt) * g_avg;
+      const double wt = (double)powf((float)tt, -0.75f);
       x_avg = (1.0 - wt) * x_avg + wt * x_t;
       if (g.tid == 0) {
         ss[0] = x_t; ss[1] = x_avg; ss[2] = g_avg; ss[3] = tt;
       }
-      double s = (t == P.num_warmup - 1) ? exp(x_avg) : exp(x_t);
-      float sf = (float)s;
+      float sf = expf((float)((t == P.num_warmup - 1) ? x_avg : x_t));
       if (!(sf >= FLT32_TINY)) sf = FLT32_TINY;  // also maps NaN to tiny
       if (sf > FLT32_MAX) sf = FLT32_MAX;
       step = sf;
@@ -312,10 +433,11 @@ struct Chain {
     double* m2 = P.s.mm_m2 + row();
     if (P.adapt_mass && middle) {  // welford update_fn
       nn += 1;
+      const double inv_n = 1.0 / (double)nn;
       for (int d = g.tid; d < D; d += NT) {
         double x = (double)z[d];
         double dpre = x - mean[d];
-        double mnew = mean[d] + dpre / nn;
+        double mnew = mean[d] + dpre * inv_n;
         mean[d] = mnew;
         m2[d] += dpre * (x - mnew);
       }
@@ -392,7 +514,7 @@ struct Chain {
       rh[d] = h;
       q[d] = z[d] + eps * (mi[d] * h);
     }
-    ctl.heur_e0 = P.s.potential_energy[c] + 0.5 * g.sum((double)kin, red);
+    ctl.heur_e0 = P.s.potential_energy[c] + 0.5 * ff_value(g.sumff(ff_from(kin), red));
     ctl.phase = PH_HEUR;
   }
   // returns true when the search is over (step size in ctl.heur_step)
@@ -406,7 +528,7 @@ struct Chain {
       float rn = rh[d] - 0.5f * eps * G[d];
       kin = fmaf(mi[d] * rn, rn, kin);
     }
-    double e_new = P.e.PE[c] + 0.5 * g.sum((double)kin, red);
+    double e_new = P.e.PE[c] + 0.5 * ff_value(g.sumff(ff_from(kin), red));
     double dE = e_new - ctl.heur_e0;
     int dir_new = (log(0.8) < -dE) ? 1 : -1;
     ctl.heur_last = ctl.heur_dir;
@@ -440,10 +562,8 @@ struct Chain {
     float* z = V(P.s.z);
     float* gz = V(P.s.z_grad);
     if (znew != z) {
-      for (int d = g.tid; d < D; d += NT) {
-        z[d] = znew[d];
-        gz[d] = gnew[d];
-      }
+      copy(z, znew);
+      copy(gz, gnew);
     }
     const int i = P.s.i[c];  // read by every thread before thread 0 advances it
     g.sync();
@@ -468,7 +588,7 @@ struct Chain {
         size_t o = (size_t)c * P.num_collect + sidx;
         if (P.col.samples) {
           float* dst = P.col.samples + o * ld;
-          for (int d = g.tid; d < D; d += NT) dst[d] = znew[d];
+          copy(dst, znew);
         }
         if (g.tid == 0) {
           if (P.col.num_steps) P.col.num_steps[o] = num_steps;
@@ -499,7 +619,7 @@ struct Chain {
     // Other chains raise the count concurrently: thread 0 reads it once and the group sum hands
     // that one reading to every thread, so all warps of a CTA-per-chain group decide alike.
     const int cnt = (g.tid == 0) ? *((volatile int32_t*)&P.done_count[ctl.iters_done - 1]) : 0;
-    return g.sum((double)cnt, red) >= (double)P.C;
+    return g.sumff(ff_from((float)cnt), red).hi >= (float)P.C;  // counts <= 2^24 are exact
   }
 
   // ----------------------------------------------------------- driver
@@ -539,12 +659,12 @@ struct Chain {
         double e_new = pe + kin;
         double dE = e_new - ctl.energy0;
         if (isnan(dE)) dE = INFINITY;
-        double acc = fmin(exp(-dE), 1.0);
+        double acc = (double)exp_min1_f(-dE);
         int div = dE > P.max_dE;
         uint32_t n = P.s.rng_key[2 * c + 1];
         uint32_t chain_id = P.s.rng_key[2 * c];
         uint4 u = draw(P.seed, chain_id, n, P_HMC_ACCEPT, 0, 0);
-        bool take = u01d(u.x) < acc;
+        bool take = u01f(u.x) < (float)acc;
         bool pend;
         if (take)
           pend = finish_transition(pe, e_new, ctl.hmc_total, acc, div, V(P.e.z_r), V(P.e.g_r));

@@ -198,123 +198,168 @@ __global__ void logreg_finish_kernel(const float* __restrict__ Q, int npts, int 
   if (lane == 0) PE[c] = ll + lp + (double)p * (0.5 * LOG_2PI + log(prior_scale));
 }
 
-// ============================================================ generic strided FP32 GEMM
-// Out[s][m][n] = sum_{k in split s} A(m,k) B(k,n).  Used by the horseshoe family.
-// Epilogue mode 1: Out = y[m] - acc, and part_rr[mtile][n] = sum_m Out^2.
-constexpr int GT = 64, GK = 16;
-__global__ void __launch_bounds__(256) gemm_strided_kernel(const float* __restrict__ A, int64_t a_m, int64_t a_k,
-                                                           const float* __restrict__ B, int64_t b_k, int64_t b_n,
-                                                           float* __restrict__ Out, int64_t o_m, int64_t o_n,
-                                                           int64_t o_split, int M, int N, int K, int k_per_split,
-                                                           int mode, const float* __restrict__ yv,
-                                                           double* __restrict__ part_rr, const int32_t* pending) {
+// ============================================================ horseshoe: FP32 GEMMs + prior terms
+// Both contractions of the Gaussian GLM run as one "NN" SGEMM, C[m][n] = sum_k A[k][m] B[k][n],
+// with A and B row-major and m/n contiguous (rows padded to a multiple of 4 floats, so every
+// tile row is float4-aligned):
+//   residuals  R[row][c]  = y[row] - sum_p Xt[p][row] Bt[p][c]       (Xt = X^T, Bt = beta^T)
+//   adjoint    GB[c][p]   = sum_row R[row][c] X[row][p]              (split over row ranges)
+// X^T and a padded X are built once per model; beta^T is packed from the chains' positions each
+// tick.  64 x 64 tiles, 16-deep K steps double-buffered through registers; 4 x 4 outputs per
+// thread.  Residual sums of squares per (row tile, chain) leave the GEMM in FP64.
+constexpr int HS_BM = 64, HS_BN = 64, HS_BK = 16;
+constexpr int HS_SPLITS = 4;  // row ranges of the adjoint GEMM (enough CTAs for 152 SMs)
+
+__global__ void __launch_bounds__(256) hs_sgemm_nn_kernel(const float* __restrict__ A, int lda,
+                                                          const float* __restrict__ B, int ldb, int M, int N,
+                                                          int K, int k_per_split, float* __restrict__ Out, int ldo,
+                                                          int64_t split_stride, const float* __restrict__ yv,
+                                                          double* __restrict__ part_rr, int ld_rr,
+                                                          const int32_t* pending) {
   if (pending && *pending == 0) return;
-  __shared__ __align__(16) float As[GK][GT];
-  __shared__ __align__(16) float Bs[GK][GT];
-  __shared__ double rr[16][GT];
+  __shared__ __align__(16) float As[2][HS_BK][HS_BM];
+  __shared__ __align__(16) float Bs[2][HS_BK][HS_BN];
+  __shared__ float rr[16][HS_BN];
   const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
-  const int m0 = blockIdx.y * GT, n0 = blockIdx.x * GT;
-  const int split = blockIdx.z;
-  const int kb = split * k_per_split;
-  const int ke = min(K, kb + k_per_split);
+  const int m0 = blockIdx.y * HS_BM, n0 = blockIdx.x * HS_BN;
+  const int kb = blockIdx.z * k_per_split, ke = min(K, kb + k_per_split);
+  // each thread stages one float4 of A and one of B per K step: row lk, columns 4*lc..4*lc+3
+  const int lk = tid >> 4, lc = (tid & 15) * 4;
+  auto load = [&](int k0, float4& av, float4& bv) {
+    const int k = k0 + lk;
+    const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
+    av = (k < ke && m0 + lc < M) ? *reinterpret_cast<const float4*>(A + (size_t)k * lda + m0 + lc) : zero;
+    bv = (k < ke && n0 + lc < N) ? *reinterpret_cast<const float4*>(B + (size_t)k * ldb + n0 + lc) : zero;
+  };
   float acc[4][4] = {};
-  for (int k0 = kb; k0 < ke; k0 += GK) {
-    for (int e = tid; e < GK * GT; e += 256) {
-      int kk, mm;
-      if (a_k == 1) { mm = e / GK; kk = e % GK; } else { kk = e / GT; mm = e % GT; }
-      int gm = m0 + mm, gk = k0 + kk;
-      As[kk][mm] = (gm < M && gk < ke) ? A[gm * a_m + gk * a_k] : 0.0f;
-      int nn;
-      if (b_k == 1) { nn = e / GK; kk = e % GK; } else { kk = e / GT; nn = e % GT; }
-      int gn = n0 + nn;
-      gk = k0 + kk;
-      Bs[kk][nn] = (gn < N && gk < ke) ? B[gk * b_k + gn * b_n] : 0.0f;
-    }
+  float4 av, bv;
+  load(kb, av, bv);
+  int buf = 0;
+  for (int k0 = kb; k0 < ke; k0 += HS_BK) {
+    *reinterpret_cast<float4*>(&As[buf][lk][lc]) = av;
+    *reinterpret_cast<float4*>(&Bs[buf][lk][lc]) = bv;
     __syncthreads();
+    if (k0 + HS_BK < ke) load(k0 + HS_BK, av, bv);  // next step's loads overlap this step's FMAs
 #pragma unroll
-    for (int kk = 0; kk < GK; ++kk) {
-      float4 av = *reinterpret_cast<const float4*>(&As[kk][ty * 4]);
-      float4 bv = *reinterpret_cast<const float4*>(&Bs[kk][tx * 4]);
-      float aa[4] = {av.x, av.y, av.z, av.w};
-      float bb[4] = {bv.x, bv.y, bv.z, bv.w};
+    for (int kk = 0; kk < HS_BK; ++kk) {
+      const float4 a4 = *reinterpret_cast<const float4*>(&As[buf][kk][ty * 4]);
+      const float4 b4 = *reinterpret_cast<const float4*>(&Bs[buf][kk][tx * 4]);
+      const float aa[4] = {a4.x, a4.y, a4.z, a4.w};
+      const float bb[4] = {b4.x, b4.y, b4.z, b4.w};
 #pragma unroll
       for (int i = 0; i < 4; ++i)
 #pragma unroll
         for (int j = 0; j < 4; ++j) acc[i][j] = fmaf(aa[i], bb[j], acc[i][j]);
     }
-    __syncthreads();
+    buf ^= 1;  // the other buffer was last read before this step's barrier
   }
-  double rrl[4] = {0, 0, 0, 0};
+  float* out = Out + (size_t)blockIdx.z * split_stride;
+  if (yv == nullptr) {
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const int m = m0 + ty * 4 + i;
+      if (m >= M) continue;
+      if (n0 + tx * 4 < N)
+        *reinterpret_cast<float4*>(out + (size_t)m * ldo + n0 + tx * 4) =
+            make_float4(acc[i][0], acc[i][1], acc[i][2], acc[i][3]);
+    }
+    return;
+  }
+  // residual epilogue: R = y - acc, and per-chain sums of R^2 over this row tile
+  float sq[4] = {0.f, 0.f, 0.f, 0.f};
 #pragma unroll
   for (int i = 0; i < 4; ++i) {
-    int gm = m0 + ty * 4 + i;
-    if (gm >= M) continue;
+    const int m = m0 + ty * 4 + i;
+    if (m >= M) continue;
+    const float y = yv[m];
+    float r[4];
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
-      int gn = n0 + tx * 4 + j;
-      if (gn >= N) continue;
-      float v = acc[i][j];
-      if (mode == 1) {
-        v = yv[gm] - v;
-        rrl[j] += (double)v * (double)v;
-      }
-      Out[split * o_split + gm * o_m + gn * o_n] = v;
+      r[j] = y - acc[i][j];
+      sq[j] = fmaf(r[j], r[j], sq[j]);
     }
+    if (n0 + tx * 4 < N) *reinterpret_cast<float4*>(out + (size_t)m * ldo + n0 + tx * 4) = make_float4(r[0], r[1], r[2], r[3]);
   }
-  if (mode == 1) {
 #pragma unroll
-    for (int j = 0; j < 4; ++j) rr[ty][tx * 4 + j] = rrl[j];
-    __syncthreads();
-    if (tid < GT && n0 + tid < N) {
-      double s = 0.0;
-      for (int k = 0; k < 16; ++k) s += rr[k][tid];
-      part_rr[(size_t)blockIdx.y * N + n0 + tid] = s;
-    }
+  for (int j = 0; j < 4; ++j) rr[ty][tx * 4 + j] = sq[j];
+  __syncthreads();
+  if (tid < HS_BN && n0 + tid < N) {
+    double t = 0.0;
+    for (int k = 0; k < 16; ++k) t += (double)rr[k][tid];
+    part_rr[(size_t)blockIdx.y * ld_rr + n0 + tid] = t;
   }
 }
 
-// horseshoe: z = [beta(P), log lambdas(P), log sigma, log tau]; CTA per point
+// Bt[p][c] = Q[c][p] (p < P, c < npts), zero in the padding; 32 x 32 tiles through shared memory.
+__global__ void __launch_bounds__(256) hs_pack_kernel(const float* __restrict__ Q, int ld, int npts, int P,
+                                                      float* __restrict__ Bt, int ldb, int prows,
+                                                      const int32_t* pending) {
+  if (pending && *pending == 0) return;
+  __shared__ float t[32][33];
+  const int c0 = blockIdx.x * 32, p0 = blockIdx.y * 32;
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  for (int k = ty; k < 32; k += 8) {
+    const int c = c0 + k, p = p0 + tx;
+    t[k][tx] = (c < npts && p < P) ? Q[(size_t)c * ld + p] : 0.0f;
+  }
+  __syncthreads();
+  for (int k = ty; k < 32; k += 8) {
+    const int p = p0 + k, c = c0 + tx;
+    if (p < prows && c < ldb) Bt[(size_t)p * ldb + c] = t[tx][k];
+  }
+}
+
+// Prior terms and the gradient of the horseshoe GLM, one CTA per chain, FP32 per coordinate with
+// float-float sums.  z = [beta(P), log lambda(P), log sigma, log tau] (sorted sites).
+//   beta_d ~ Normal(0, tau lambda_d): 0.5 b^2/s^2 + log s, s = tau lambda  (the log lambda cancels
+//   against the Exp log-det);  lambda_d, tau ~ HalfCauchy(1);  sigma ~ HalfNormal(1).
+// log(1 + lambda^2) = 2 max(l, 0) + log1p(e^{-2|l|}) and 2 lambda^2/(1 + lambda^2) = 2 / (1 + e^{-2l})
+// stay finite for any l.
 __global__ void __launch_bounds__(256) horseshoe_finish_kernel(const float* __restrict__ Q, int npts, int ld, int P,
                                                                int64_t N, const float* __restrict__ part_gb,
-                                                               int splits, const double* __restrict__ part_rr,
-                                                               int mtiles, double* __restrict__ PE,
+                                                               int splits, int ldg, const double* __restrict__ part_rr,
+                                                               int ld_rr, int mtiles, double* __restrict__ PE,
                                                                float* __restrict__ G, const int32_t* pending) {
   if (pending && *pending == 0) return;
   __shared__ double red[16];
-  int c = blockIdx.x;
-  int tid = threadIdx.x;
+  const int c = blockIdx.x, tid = threadIdx.x;
   Group<256> g{tid};
   const float* z = Q + (size_t)c * ld;
   float* gz = G + (size_t)c * ld;
-  double lsig = z[2 * P], ltau = z[2 * P + 1];
-  double sig = exp(lsig), tau = exp(ltau);
-  double rrs = 0.0;
-  for (int t = tid; t < mtiles; t += 256) rrs += part_rr[(size_t)t * npts + c];
-  double RR = g.sum(rrs, red);
-  double inv_s2 = 1.0 / (sig * sig);
-  double lp = 0.0, gt = 0.0;
+  const float lsig = z[2 * P], ltau = z[2 * P + 1];
+  const float inv_sig2 = expf(-2.0f * lsig);
+  double rrd = 0.0;  // this thread's row tiles (at most a few), then a float-float pair
+  for (int t = tid; t < mtiles; t += 256) rrd += part_rr[(size_t)t * ld_rr + c];
+  const float rr_hi = (float)rrd;
+  const FF rr_ff{rr_hi, (float)(rrd - (double)rr_hi)};
+  Comp32 lp{0.0f, 0.0f}, gt{0.0f, 0.0f};
   for (int d = tid; d < P; d += 256) {
-    double b = z[d], ll = z[P + d];
-    double lam = exp(ll);
-    double s = tau * lam;
-    double gb = 0.0;
-    for (int k = 0; k < splits; ++k) gb += (double)part_gb[((size_t)k * npts + c) * P + d];
-    double b2s = b * b / (s * s);
-    gz[d] = (float)(b / (s * s) - gb * inv_s2);
-    gz[P + d] = (float)(-b2s + 2.0 * lam * lam / (1.0 + lam * lam));
-    lp += -0.5 * b2s - log(s) - 0.5 * LOG_2PI;                 // Normal(beta; 0, tau*lam)
-    lp += -LOG_PI - log1p(lam * lam) + LOG_2 + ll;             // HalfCauchy(lam; 1) + log-det
-    gt += 1.0 - b2s;
+    const float b = z[d], l = z[P + d];
+    float gb = 0.0f;
+    for (int k = 0; k < splits; ++k) gb += part_gb[((size_t)k * npts + c) * ldg + d];
+    const float inv_s2 = expf(-2.0f * (ltau + l));
+    const float b2s = b * b * inv_s2;
+    const float e2 = expf(-2.0f * fabsf(l));
+    const float log1p_lam2 = 2.0f * fmaxf(l, 0.0f) + log1pf(e2);
+    const float hc = (l >= 0.0f) ? 2.0f / (1.0f + e2) : 2.0f * e2 / (1.0f + e2);  // 2 lam^2 / (1 + lam^2)
+    gz[d] = b * inv_s2 - gb * inv_sig2;
+    gz[P + d] = hc - b2s;
+    lp.add(-0.5f * b2s - log1p_lam2);
+    gt.add(1.0f - b2s);
   }
-  double2 t2 = g.sum2(make_double2(lp, gt), red);
+  FF flp = comp_ff(lp), fgt = comp_ff(gt);
+  g.sum2ff(flp, fgt, red);
+  FF frr = g.sumff(rr_ff, red);
   if (tid == 0) {
-    double total = t2.x;
-    total += -0.5 * sig * sig - 0.5 * LOG_2PI + LOG_2 + lsig;  // HalfNormal(sigma; 1) + log-det
-    total += -LOG_PI - log1p(tau * tau) + LOG_2 + ltau;        // HalfCauchy(tau; 1) + log-det
-    total += -0.5 * RR * inv_s2 - (double)N * lsig - 0.5 * (double)N * LOG_2PI;
+    const double RR = ff_value(frr), dlsig = lsig, dltau = ltau;
+    const double sig = exp(dlsig), tau = exp(dltau), inv_s2 = exp(-2.0 * dlsig);
+    double total = ff_value(flp) + (double)P * (LOG_2 - LOG_PI - 0.5 * LOG_2PI - dltau);
+    total += -0.5 * sig * sig - 0.5 * LOG_2PI + LOG_2 + dlsig;  // HalfNormal(sigma; 1) + log-det
+    total += -LOG_PI - log1p(tau * tau) + LOG_2 + dltau;        // HalfCauchy(tau; 1) + log-det
+    total += -0.5 * RR * inv_s2 - (double)N * dlsig - 0.5 * (double)N * LOG_2PI;
     PE[c] = -total;
     gz[2 * P] = (float)(sig * sig - 1.0 - RR * inv_s2 + (double)N);
-    gz[2 * P + 1] = (float)(t2.y + 2.0 * tau * tau / (1.0 + tau * tau) - 1.0);
+    gz[2 * P + 1] = (float)(ff_value(fgt) + 2.0 * tau * tau / (1.0 + tau * tau) - 1.0);
   }
 }
 
@@ -359,10 +404,12 @@ cudaError_t ensure_potential_scratch(ModelDev& m, int points) {
     e = cudaMalloc(&m.part_g, sizeof(float) * (size_t)rg * points * 64);
     if (e == cudaSuccess) e = cudaMalloc(&m.part_ll, sizeof(double) * (size_t)rg * points);
   } else if (m.family == 3) {
-    int mt = (int)((m.n + GT - 1) / GT);
-    e = cudaMalloc(&m.resid, sizeof(float) * (size_t)m.n * points);
-    if (e == cudaSuccess) e = cudaMalloc(&m.part_rr, sizeof(double) * (size_t)mt * points);
-    if (e == cudaSuccess) e = cudaMalloc(&m.part_gb, sizeof(float) * (size_t)4 * points * m.p);
+    const int cp = pad4(points), pp = pad4(m.p);
+    const int mt = (int)((m.n + HS_BM - 1) / HS_BM);
+    e = cudaMalloc(&m.resid, sizeof(float) * (size_t)m.n * cp);
+    if (e == cudaSuccess) e = cudaMalloc(&m.part_rr, sizeof(double) * (size_t)mt * cp);
+    if (e == cudaSuccess) e = cudaMalloc(&m.part_gb, sizeof(float) * (size_t)HS_SPLITS * points * pp);
+    if (e == cudaSuccess) e = cudaMalloc(&m.hs_bt, sizeof(float) * (size_t)pp * cp);
   }
   if (e == cudaSuccess) {
     m.scratch_points = points;
@@ -377,6 +424,8 @@ void free_potential_scratch(ModelDev& m) {
   cudaFree(m.resid);
   cudaFree(m.part_rr);
   cudaFree(m.part_gb);
+  cudaFree(m.hs_bt);
+  m.hs_bt = nullptr;
   m.part_g = nullptr;
   m.part_ll = nullptr;
   m.resid = nullptr;
@@ -418,21 +467,22 @@ cudaError_t launch_potential(ModelDev& m, const float* Q, int npts, double* PE, 
       break;
     }
     case 3: {
-      int P = m.p;
-      int M = (int)m.n;
-      int mt = (M + GT - 1) / GT;
-      // R[n][c] = y[n] - sum_p X[n][p] beta_c[p]
-      dim3 g1((npts + GT - 1) / GT, mt, 1);
-      gemm_strided_kernel<<<g1, 256, 0, st>>>(m.x, P, 1, Q, 1, ld, m.resid, npts, 1, 0, M, npts, P, P, 1, m.y,
-                                              m.part_rr, pending);
-      // GB[s][c][p] = sum_{n in split s} R[n][c] X[n][p]
-      int splits = 4;
-      int kps = (((M + splits - 1) / splits) + GK - 1) / GK * GK;
-      dim3 g2((P + GT - 1) / GT, (npts + GT - 1) / GT, splits);
-      gemm_strided_kernel<<<g2, 256, 0, st>>>(m.resid, 1, npts, m.x, P, 1, m.part_gb, P, 1, (int64_t)npts * P,
-                                              npts, P, M, kps, 0, nullptr, nullptr, pending);
-      horseshoe_finish_kernel<<<npts, 256, 0, st>>>(Q, npts, ld, P, m.n, m.part_gb, splits, m.part_rr, mt, PE, G,
-                                                    pending);
+      const int P = m.p, M = (int)m.n, cp = pad4(npts), pp = pad4(P);
+      const int mt = (M + HS_BM - 1) / HS_BM;
+      // beta^T for the chains' query points
+      dim3 gp((cp + 31) / 32, (pp + 31) / 32);
+      hs_pack_kernel<<<gp, 256, 0, st>>>(Q, ld, npts, P, m.hs_bt, cp, pp, pending);
+      // R[row][c] = y[row] - sum_p X[row][p] beta_c[p]
+      dim3 g1((npts + HS_BN - 1) / HS_BN, mt, 1);
+      hs_sgemm_nn_kernel<<<g1, 256, 0, st>>>(m.hs_xt, pad4(M), m.hs_bt, cp, M, npts, P, P, m.resid, cp, 0, m.y,
+                                             m.part_rr, cp, pending);
+      // GB[s][c][p] = sum_{row in split s} R[row][c] X[row][p]
+      const int kps = (((M + HS_SPLITS - 1) / HS_SPLITS) + HS_BK - 1) / HS_BK * HS_BK;
+      dim3 g2((P + HS_BN - 1) / HS_BN, (npts + HS_BM - 1) / HS_BM, HS_SPLITS);
+      hs_sgemm_nn_kernel<<<g2, 256, 0, st>>>(m.resid, cp, m.hs_xp, pp, npts, P, M, kps, m.part_gb, pp,
+                                             (int64_t)npts * pp, nullptr, nullptr, 0, pending);
+      horseshoe_finish_kernel<<<npts, 256, 0, st>>>(Q, npts, ld, P, m.n, m.part_gb, HS_SPLITS, pp, m.part_rr, cp,
+                                                    mt, PE, G, pending);
       break;
     }
     case 4:

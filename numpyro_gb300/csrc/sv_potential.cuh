@@ -16,9 +16,10 @@
 // walk is stored only at chunk starts (one checkpoint per thread, from a block-wide exclusive scan
 // of the chunk totals) and recomputed inside the chunk from its checkpoint.  The reverse pass
 // needs the suffix sums of a_t: a block-wide reverse exclusive scan of the chunk totals gives each
-// thread its starting suffix, and a_t itself is parked in the gradient row (the only T-length
-// buffer touched) between the passes.  Running sums inside a chunk are compensated FP32
-// (two-sum, Knuth TAOCP vol. 2 4.2.2); chunk totals are scanned and reduced in FP64.
+// thread its starting suffix; a_t itself stays in registers between the passes (or, for chunks
+// too long for registers, is parked in the gradient row).  Running sums inside a chunk are compensated FP32
+// (two-sum, Knuth TAOCP vol. 2 4.2.2); chunk totals are scanned and reduced as float-float
+// pairs.
 #pragma once
 #include <cuda_runtime.h>
 #include <math.h>
@@ -34,44 +35,44 @@ constexpr double SV_LOG_PI = 1.1447298858494002;
 template <int NT>
 struct SvSmem {
   double red[16];        // Group<256> reductions
-  double special[4];     // lgamma(nu/2), lgamma((nu+1)/2), digamma(nu/2), digamma((nu+1)/2)
-  double warp_tot[2][NT / 32];
+  double special[9];     // lgamma(nu/2), lgamma((nu+1)/2), digamma(nu/2), digamma((nu+1)/2),
+                         // nu, 1/nu, s, 1/s, log(s_rate) + log(nu_rate)
+  float2 warp_tot[2][NT / 32];
 };
 
-// The four FP64 special functions of nu, each on lane 0 of its own warp so they run side by side
-// with the element loop; read after the next barrier.
+// The FP64 scalar factors of the potential, each group on lane 0 of its own warp so they run side
+// by side with the element loop; thread 0 reads them after the reductions' barriers.
 template <int NT>
-__device__ __forceinline__ void sv_special_functions(double nu, int tid, double* special) {
-  static_assert(NT >= 128, "needs four warps");
-  if (tid == 0) special[0] = lgamma(0.5 * nu);
-  else if (tid == 32) special[1] = lgamma(0.5 * (nu + 1.0));
-  else if (tid == 64) special[2] = digamma_d(0.5 * nu);
-  else if (tid == 96) special[3] = digamma_d(0.5 * (nu + 1.0));
+__device__ __forceinline__ void sv_special_functions(float lnuf, float lsf, double s_rate, double nu_rate, int tid,
+                                                     double* special) {
+  static_assert(NT >= 256, "needs six warps");
+  if ((tid & 31) != 0) return;
+  const double nu = exp((double)lnuf);
+  switch (tid >> 5) {
+    case 0: special[0] = lgamma(0.5 * nu); break;
+    case 1: special[1] = lgamma(0.5 * (nu + 1.0)); break;
+    case 2: special[2] = digamma_d(0.5 * nu); break;
+    case 3: special[3] = digamma_d(0.5 * (nu + 1.0)); break;
+    case 4: special[4] = nu; special[5] = 1.0 / nu; break;
+    case 5: {
+      const double s = exp((double)lsf);
+      special[6] = s;
+      special[7] = 1.0 / s;
+      special[8] = log(s_rate) + log(nu_rate);
+      break;
+    }
+    default: break;
+  }
 }
 
 // d/dlnu of U (both parameterisations): nu-dependent StudentT terms summed over T plus the prior.
-__device__ __forceinline__ float sv_grad_lnu(double nu, double S_l1p, double S_frac, double T, double nu_rate,
+__device__ __forceinline__ float sv_grad_lnu(double S_l1p, double S_frac, double T, double nu_rate,
                                              const double* special) {
-  double dnu = -0.5 * S_l1p + 0.5 * (nu + 1.0) / nu * S_frac - 0.5 * T / nu - 0.5 * T * special[2] +
+  const double nu = special[4], inv_nu = special[5];
+  double dnu = -0.5 * S_l1p + 0.5 * (nu + 1.0) * inv_nu * S_frac - 0.5 * T * inv_nu - 0.5 * T * special[2] +
                0.5 * T * special[3] - nu_rate;
   return (float)(-(dnu * nu + 1.0));
 }
-
-// Compensated FP32 accumulator (two-sum; the error term is carried separately).
-struct Comp32 {
-  float s, c;
-  __device__ __forceinline__ void add(float x) {
-    float t = s + x;
-    float bp = t - s;
-    c += (s - (t - bp)) + (x - bp);
-    s = t;
-  }
-  __device__ __forceinline__ float value() const { return s + c; }
-};
-
-// Each thread's share of the T-length sums is accumulated in compensated FP32 and the shares
-// are summed across the CTA in FP64.
-__device__ __forceinline__ double comp_total(const Comp32& a) { return (double)a.s + (double)a.c; }
 
 // The potentials are compiled out of line: the tick and persistent kernels then run one and
 // the same instruction sequence (inlined into different kernels, floating-point contraction
@@ -82,134 +83,188 @@ __device__ __noinline__ void sv_potential_block(const float* z, float* g, double
                                                    const float* __restrict__ ret, double s_rate, double nu_rate,
                                                    int tid, SvSmem<NT>& sm) {
   Group<NT> grp{tid};
-  double lnu = z[T], ls = z[T + 1];
-  double nu = exp(lnu), s = exp(ls);
-  sv_special_functions<NT>(nu, tid, sm.special);
-  float nuf = (float)nu;
-  float inv_s2 = (float)(1.0 / (s * s));
+  // FP32 nu and 1/s^2 for the element loop; FP64 nu and s only where the scalar terms need them
+  const float lnuf = z[T], lsf = z[T + 1];
+  const float nuf = expf(lnuf), sf = expf(lsf);
+  const float inv_s2 = 1.0f / (sf * sf), inv_nuf = 1.0f / nuf;
+  sv_special_functions<NT>(lnuf, lsf, s_rate, nu_rate, tid, sm.special);
   Comp32 sdd{0.0f, 0.0f}, sl1p{0.0f, 0.0f}, sfrac{0.0f, 0.0f}, sh{0.0f, 0.0f};
-  for (int t = tid; t < T; t += NT) {
-    float h = z[t];
-    float dprev = (t == 0) ? h : h - z[t - 1];
-    float dnext = (t + 1 < T) ? z[t + 1] - h : 0.0f;
-    float rt = ret[t];
-    float yv = rt * expf(-h);
-    float y2 = yv * yv;
-    float q = y2 / nuf;
-    float frac = y2 / (nuf + y2);
-    sdd.add(dprev * dprev);
-    sl1p.add(log1pf(q));
-    sfrac.add(frac);
-    sh.add(h);
-    g[t] = (dprev - dnext) * inv_s2 + 1.0f - (nuf + 1.0f) * frac;
+  constexpr int U = 4;  // loads of U steps are issued before their gradient stores
+  for (int t0 = tid; t0 < T; t0 += U * NT) {
+    float hv[U], hp[U], hn[U], rv[U];
+#pragma unroll
+    for (int k = 0; k < U; ++k) {
+      const int t = t0 + k * NT;
+      const bool in = t < T;
+      hv[k] = in ? z[t] : 0.0f;
+      hp[k] = (in && t > 0) ? z[t - 1] : 0.0f;
+      hn[k] = (t + 1 < T) ? z[t + 1] : 0.0f;
+      rv[k] = in ? ret[t] : 0.0f;
+    }
+#pragma unroll
+    for (int k = 0; k < U; ++k) {
+      const int t = t0 + k * NT;
+      if (t >= T) continue;
+      const float h = hv[k];
+      const float dprev = (t == 0) ? h : h - hp[k];
+      const float dnext = (t + 1 < T) ? hn[k] - h : 0.0f;
+      const float yv = rv[k] * expf(-h);
+      const float y2 = yv * yv;
+      const float q = y2 * inv_nuf;
+      const float frac = __fdividef(y2, nuf + y2);
+      sdd.add(dprev * dprev);
+      sl1p.add(log1pf(q));
+      sfrac.add(frac);
+      sh.add(h);
+      g[t] = (dprev - dnext) * inv_s2 + 1.0f - (nuf + 1.0f) * frac;
+    }
   }
-  double2 a = grp.sum2(make_double2(comp_total(sdd), comp_total(sl1p)), sm.red);
-  double2 b = grp.sum2(make_double2(comp_total(sfrac), comp_total(sh)), sm.red);
+  FF f_dd = comp_ff(sdd), f_l1p = comp_ff(sl1p), f_frac = comp_ff(sfrac), f_h = comp_ff(sh);
+  grp.sum2ff(f_dd, f_l1p, sm.red);
+  grp.sum2ff(f_frac, f_h, sm.red);
   if (tid == 0) {
-    double S_dd = a.x, S_l1p = a.y, S_frac = b.x, S_h = b.y;
-    double lp = log(s_rate) - s_rate * s + ls;
-    lp += log(nu_rate) - nu_rate * nu + lnu;
-    lp += -0.5 * S_dd / (s * s) - (double)T * ls - 0.5 * (double)T * SV_LOG_2PI;
+    const double lnu = lnuf, ls = lsf, nu = sm.special[4], s = sm.special[6], inv_s = sm.special[7];
+    double S_dd = ff_value(f_dd), S_l1p = ff_value(f_l1p), S_frac = ff_value(f_frac), S_h = ff_value(f_h);
+    double lp = sm.special[8] - s_rate * s + ls - nu_rate * nu + lnu;
+    lp += -0.5 * S_dd * (inv_s * inv_s) - (double)T * ls - 0.5 * (double)T * SV_LOG_2PI;
     double zc = 0.5 * lnu + 0.5 * SV_LOG_PI + sm.special[0] - sm.special[1];
     lp += -0.5 * (nu + 1.0) * S_l1p - S_h - (double)T * zc;
     *pe_out = -lp;
-    g[T] = sv_grad_lnu(nu, S_l1p, S_frac, (double)T, nu_rate, sm.special);
-    double ds = S_dd / (s * s * s) - (double)T / s - s_rate;
+    g[T] = sv_grad_lnu(S_l1p, S_frac, (double)T, nu_rate, sm.special);
+    double ds = S_dd * (inv_s * inv_s * inv_s) - (double)T * inv_s - s_rate;
     g[T + 1] = (float)(-(ds * s + 1.0));
   }
 }
 
-// Block-wide exclusive scans of one double per thread (forward: sum over lower threads;
-// reverse: sum over higher threads).  Contain two barriers; `wt` holds NT/32 doubles.
+// Block-wide exclusive scans of one float-float pair per thread (forward: sum over lower
+// threads; reverse: sum over higher threads).  Lanes combine by shuffles, warps through `wt`
+// (NT/32 pairs); each contains two barriers.
 template <int NT>
-__device__ __forceinline__ double block_excl_scan(double v, int tid, double* wt) {
+__device__ __forceinline__ FF block_excl_scan(FF v, int tid, float2* wt) {
   const int lane = tid & 31, w = tid >> 5;
-  double incl = v;
+  FF excl{0.0f, 0.0f};
 #pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    double x = __shfl_up_sync(0xffffffffu, incl, o);
-    if (lane >= o) incl += x;
+  for (int o = 1; o < 32; o <<= 1) {  // inclusive lane scan of v, then shift by one lane
+    FF x{__shfl_up_sync(0xffffffffu, v.hi, o), __shfl_up_sync(0xffffffffu, v.lo, o)};
+    if (lane >= o) v = ff_add(x, v);
   }
-  if (lane == 31) wt[w] = incl;
+  excl.hi = __shfl_up_sync(0xffffffffu, v.hi, 1);
+  excl.lo = __shfl_up_sync(0xffffffffu, v.lo, 1);
+  if (lane == 0) excl = FF{0.0f, 0.0f};
+  if (lane == 31) wt[w] = make_float2(v.hi, v.lo);
   __syncthreads();
-  double off = 0.0;
-  for (int k = 0; k < w; ++k) off += wt[k];
+  FF off{0.0f, 0.0f};
+  for (int k = 0; k < w; ++k) off = ff_add(off, FF{wt[k].x, wt[k].y});
   __syncthreads();
-  return off + incl - v;
+  return ff_add(off, excl);
 }
 template <int NT>
-__device__ __forceinline__ double block_excl_rscan(double v, int tid, double* wt) {
+__device__ __forceinline__ FF block_excl_rscan(FF v, int tid, float2* wt) {
   const int lane = tid & 31, w = tid >> 5;
-  double incl = v;
+  FF excl{0.0f, 0.0f};
 #pragma unroll
   for (int o = 1; o < 32; o <<= 1) {
-    double x = __shfl_down_sync(0xffffffffu, incl, o);
-    if (lane + o < 32) incl += x;
+    FF x{__shfl_down_sync(0xffffffffu, v.hi, o), __shfl_down_sync(0xffffffffu, v.lo, o)};
+    if (lane + o < 32) v = ff_add(v, x);
   }
-  if (lane == 0) wt[w] = incl;
+  excl.hi = __shfl_down_sync(0xffffffffu, v.hi, 1);
+  excl.lo = __shfl_down_sync(0xffffffffu, v.lo, 1);
+  if (lane == 31) excl = FF{0.0f, 0.0f};
+  if (lane == 0) wt[w] = make_float2(v.hi, v.lo);
   __syncthreads();
-  double off = 0.0;
-  for (int k = NT / 32 - 1; k > w; --k) off += wt[k];
+  FF off{0.0f, 0.0f};
+  for (int k = NT / 32 - 1; k > w; --k) off = ff_add(off, FF{wt[k].x, wt[k].y});
   __syncthreads();
-  return off + incl - v;
+  return ff_add(off, excl);
 }
 
-// Non-centred GRW (h = s * cumsum(h_base)).  z/g are the chain's rows.
+// Non-centred GRW (h = s * cumsum(h_base)).  z/g are the chain's rows.  Chunks of at most
+// SV_REG_CHUNK steps (T <= 4096 with 256 threads) are held in registers.
+constexpr int SV_REG_CHUNK = 16;
 template <int NT>
 __device__ __noinline__ void sv_nc_potential_block(const float* z, float* g, double* pe_out, int T,
                                                       const float* __restrict__ ret, double s_rate,
                                                       double nu_rate, int tid, SvSmem<NT>& sm) {
   Group<NT> grp{tid};
-  double lnu = z[T], ls = z[T + 1];
-  double nu = exp(lnu), s = exp(ls);
-  sv_special_functions<NT>(nu, tid, sm.special);
-  const float nuf = (float)nu, sf = (float)s;
+  const float lnuf = z[T], lsf = z[T + 1];
+  const float nuf = expf(lnuf), sf = expf(lsf), inv_nuf = 1.0f / nuf;
+  sv_special_functions<NT>(lnuf, lsf, s_rate, nu_rate, tid, sm.special);
   const int chunk = (T + NT - 1) / NT;
   const int t0 = min(T, tid * chunk), t1 = min(T, t0 + chunk);
-  // chunk total of h_base -> checkpoint S_{t0-1} (exclusive scan)
-  Comp32 tot{0.0f, 0.0f};
-  for (int t = t0; t < t1; ++t) tot.add(z[t]);
-  double ck = block_excl_scan<NT>(comp_total(tot), tid, sm.warp_tot[0]);
-  // forward pass: recompute the walk from the checkpoint, park a_t in g
-  Comp32 S{(float)ck, (float)(ck - (double)(float)ck)};
   Comp32 sl1p{0.0f, 0.0f}, sfrac{0.0f, 0.0f}, sh{0.0f, 0.0f}, sas{0.0f, 0.0f}, se2{0.0f, 0.0f},
       atot{0.0f, 0.0f};
-  for (int t = t0; t < t1; ++t) {
-    const float e = z[t];
+  // one step of the forward pass: extend the walk, accumulate, return a_t
+  auto forward_step = [&](Comp32& S, float e, float r) -> float {
     S.add(e);
     const float St = S.value();
     const float h = sf * St;
-    const float yv = ret[t] * expf(-h);
+    const float yv = r * expf(-h);
     const float y2 = yv * yv;
-    const float frac = y2 / (nuf + y2);
+    const float frac = __fdividef(y2, nuf + y2);
     const float at = (nuf + 1.0f) * frac - 1.0f;  // d log p(r_t | h_t) / d h_t
-    sl1p.add(log1pf(y2 / nuf));
+    sl1p.add(log1pf(y2 * inv_nuf));
     sfrac.add(frac);
     sh.add(h);
     sas.add(at * St);
     se2.add(e * e);
     atot.add(at);
-    g[t] = at;
+    return at;
+  };
+  if (chunk <= SV_REG_CHUNK) {
+    // the chunk's h_base, returns and a_t stay in registers between the passes
+    float ev[SV_REG_CHUNK], rv[SV_REG_CHUNK], av[SV_REG_CHUNK];
+#pragma unroll
+    for (int i = 0; i < SV_REG_CHUNK; ++i) {
+      const bool in = t0 + i < t1;
+      ev[i] = in ? z[t0 + i] : 0.0f;
+      rv[i] = in ? ret[t0 + i] : 0.0f;
+    }
+    // chunk total of h_base -> checkpoint S_{t0-1} (exclusive scan)
+    Comp32 tot{0.0f, 0.0f};
+#pragma unroll
+    for (int i = 0; i < SV_REG_CHUNK; ++i)
+      if (t0 + i < t1) tot.add(ev[i]);
+    const FF ck = block_excl_scan<NT>(comp_ff(tot), tid, sm.warp_tot[0]);
+    Comp32 S{ck.hi, ck.lo};
+#pragma unroll
+    for (int i = 0; i < SV_REG_CHUNK; ++i) av[i] = (t0 + i < t1) ? forward_step(S, ev[i], rv[i]) : 0.0f;
+    // reverse pass: suffix sums of a_t from the thread's starting suffix
+    const FF suf = block_excl_rscan<NT>(comp_ff(atot), tid, sm.warp_tot[1]);
+    Comp32 A{suf.hi, suf.lo};
+#pragma unroll
+    for (int i = SV_REG_CHUNK - 1; i >= 0; --i) {
+      if (t0 + i >= t1) continue;
+      A.add(av[i]);
+      g[t0 + i] = ev[i] - sf * A.value();
+    }
+  } else {
+    // long walks: a_t is parked in the gradient row between the passes
+    Comp32 tot{0.0f, 0.0f};
+    for (int t = t0; t < t1; ++t) tot.add(z[t]);
+    const FF ck = block_excl_scan<NT>(comp_ff(tot), tid, sm.warp_tot[0]);
+    Comp32 S{ck.hi, ck.lo};
+    for (int t = t0; t < t1; ++t) g[t] = forward_step(S, z[t], ret[t]);
+    const FF suf = block_excl_rscan<NT>(comp_ff(atot), tid, sm.warp_tot[1]);
+    Comp32 A{suf.hi, suf.lo};
+    for (int t = t1 - 1; t >= t0; --t) {
+      A.add(g[t]);
+      g[t] = z[t] - sf * A.value();
+    }
   }
-  // reverse pass: suffix sums of a_t from the thread's starting suffix
-  const double suf = block_excl_rscan<NT>(comp_total(atot), tid, sm.warp_tot[1]);
-  Comp32 A{(float)suf, (float)(suf - (double)(float)suf)};
-  for (int t = t1 - 1; t >= t0; --t) {
-    A.add(g[t]);
-    g[t] = z[t] - sf * A.value();
-  }
-  double2 r1 = grp.sum2(make_double2(comp_total(sl1p), comp_total(sfrac)), sm.red);
-  double2 r2 = grp.sum2(make_double2(comp_total(sh), comp_total(sas)), sm.red);
-  double r3 = grp.sum(comp_total(se2), sm.red);
+  FF f_l1p = comp_ff(sl1p), f_frac = comp_ff(sfrac), f_h = comp_ff(sh), f_as = comp_ff(sas);
+  grp.sum2ff(f_l1p, f_frac, sm.red);
+  grp.sum2ff(f_h, f_as, sm.red);
+  const FF f_e2 = grp.sumff(comp_ff(se2), sm.red);
   if (tid == 0) {
-    double S_l1p = r1.x, S_frac = r1.y, S_h = r2.x, S_as = r2.y, S_e2 = r3;
-    double lp = log(s_rate) - s_rate * s + ls;
-    lp += log(nu_rate) - nu_rate * nu + lnu;
+    const double lnu = lnuf, ls = lsf, nu = sm.special[4], s = sm.special[6];
+    double S_l1p = ff_value(f_l1p), S_frac = ff_value(f_frac), S_h = ff_value(f_h), S_as = ff_value(f_as),
+           S_e2 = ff_value(f_e2);
+    double lp = sm.special[8] - s_rate * s + ls - nu_rate * nu + lnu;
     lp += -0.5 * S_e2 - 0.5 * (double)T * SV_LOG_2PI;
     double zc = 0.5 * lnu + 0.5 * SV_LOG_PI + sm.special[0] - sm.special[1];
     lp += -0.5 * (nu + 1.0) * S_l1p - S_h - (double)T * zc;
     *pe_out = -lp;
-    g[T] = sv_grad_lnu(nu, S_l1p, S_frac, (double)T, nu_rate, sm.special);
+    g[T] = sv_grad_lnu(S_l1p, S_frac, (double)T, nu_rate, sm.special);
     g[T + 1] = (float)(-s * S_as + s_rate * s - 1.0);
   }
 }
