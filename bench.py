@@ -49,7 +49,7 @@ def parse():
                    help="potential: time only the dominant kernel (U and dU for every chain)")
     p.add_argument("--reps", type=int, default=20)
     p.add_argument("--workload", default="logreg",
-                   choices=["logreg", "eight_schools", "uneven_hier", "horseshoe", "sv", "sv_nc"],
+                   choices=["logreg", "eight_schools", "uneven_hier", "horseshoe", "horseshoe_nc", "sv", "sv_nc"],
                    help="non-default workloads: a full warmup+sampling run of that model family")
     p.add_argument("--samples", type=int, default=None, help="sampling iterations of a --workload run")
     return p.parse_args()
@@ -72,10 +72,11 @@ def run_workload(args):
         # 200 draws keep the collected [16384, S, 258] draws (about 3.4 GB) small enough to copy
         model, C, W, S = models.HierarchicalNormal(datasets=ds), 4 * len(ds), 1000, 200
         shape = "4096 datasets, J in [4,256], 16384 chains"
-    elif w == "horseshoe":
+    elif w in ("horseshoe", "horseshoe_nc"):
         X, y, _ = datasets.horseshoe_data(seed=0)
-        model, C, W, S = models.HorseshoeRegression(X, y), 256, 300, 300
-        shape = "N=2000, P=1000 (D=2002), 256 chains"
+        nc = w == "horseshoe_nc"
+        model, C, W, S = models.HorseshoeRegression(X, y, noncentered=nc), 256, 500, 500
+        shape = "N=2000, P=1000 (D=2002), 256 chains, %s beta" % ("non-centred" if nc else "centred")
     else:
         r, _ = datasets.sv_returns(seed=0)
         nc = w == "sv_nc"

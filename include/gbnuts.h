@@ -48,6 +48,8 @@ extern "C" {
 #define GBN_FAMILY_HIER_NC 1   /* non-centred hierarchical normal, many datasets  */
 #define GBN_FAMILY_LOGREG 2    /* Bernoulli-logit GLM, Normal(0,1) prior          */
 #define GBN_FAMILY_HORSESHOE 3 /* Gaussian GLM, horseshoe prior                   */
+/* GBN_FAMILY_HORSESHOE hyper: [0] = 1 selects unscaled_betas ~ Normal(0, 1), beta = tau lambda
+ * unscaled_betas (0: beta ~ Normal(0, tau lambda) sampled directly). */
 #define GBN_FAMILY_SV 4        /* Gaussian random walk + StudentT volatility      */
 /* GBN_FAMILY_SV hyper: [0] s rate (Exponential), [1] nu rate (Exponential), [2] = 1 selects the
  * non-centred walk h = s * cumsum(h_base), h_base ~ Normal(0, 1)^T (0: centred, as numpyro's

@@ -290,9 +290,10 @@ __global__ void __launch_bounds__(256) hs_sgemm_nn_kernel(const float* __restric
   }
 }
 
-// Bt[p][c] = Q[c][p] (p < P, c < npts), zero in the padding; 32 x 32 tiles through shared memory.
+// Bt[p][c] = beta_c[p] (p < P, c < npts), zero in the padding; 32 x 32 tiles through shared memory.
+// Centred: beta is z[0:P].  Non-centred: beta = exp(log tau + log lambda) * unscaled_beta.
 __global__ void __launch_bounds__(256) hs_pack_kernel(const float* __restrict__ Q, int ld, int npts, int P,
-                                                      float* __restrict__ Bt, int ldb, int prows,
+                                                      int noncentred, float* __restrict__ Bt, int ldb, int prows,
                                                       const int32_t* pending) {
   if (pending && *pending == 0) return;
   __shared__ float t[32][33];
@@ -300,7 +301,12 @@ __global__ void __launch_bounds__(256) hs_pack_kernel(const float* __restrict__ 
   const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
   for (int k = ty; k < 32; k += 8) {
     const int c = c0 + k, p = p0 + tx;
-    t[k][tx] = (c < npts && p < P) ? Q[(size_t)c * ld + p] : 0.0f;
+    float v = 0.0f;
+    if (c < npts && p < P) {
+      const float* z = Q + (size_t)c * ld;
+      v = noncentred ? expf(z[P + 1] + z[p]) * z[P + 2 + p] : z[p];
+    }
+    t[k][tx] = v;
   }
   __syncthreads();
   for (int k = ty; k < 32; k += 8) {
@@ -310,7 +316,11 @@ __global__ void __launch_bounds__(256) hs_pack_kernel(const float* __restrict__ 
 }
 
 // Prior terms and the gradient of the horseshoe GLM, one CTA per chain, FP32 per coordinate with
-// float-float sums.  z = [beta(P), log lambda(P), log sigma, log tau] (sorted sites).
+// float-float sums.  Centred: z = [beta(P), log lambda(P), log sigma, log tau] (sorted sites).
+// Non-centred (unscaled_betas ~ Normal(0, 1), beta = tau lambda unscaled_beta, as
+// examples/horseshoe_regression.py:33-49): z = [log lambda(P), log sigma, log tau, unscaled_beta(P)];
+// with g = X^T R / sigma^2: dU/d unscaled_d = eta_d - tau lambda_d g_d, dU/d log lambda_d =
+// -beta_d g_d + 2 lambda^2/(1+lambda^2) - 1, dU/d log tau = -sum_d beta_d g_d + 2 tau^2/(1+tau^2) - 1.
 //   beta_d ~ Normal(0, tau lambda_d): 0.5 b^2/s^2 + log s, s = tau lambda  (the log lambda cancels
 //   against the Exp log-det);  lambda_d, tau ~ HalfCauchy(1);  sigma ~ HalfNormal(1).
 // log(1 + lambda^2) = 2 max(l, 0) + log1p(e^{-2|l|}) and 2 lambda^2/(1 + lambda^2) = 2 / (1 + e^{-2l})
@@ -318,15 +328,17 @@ __global__ void __launch_bounds__(256) hs_pack_kernel(const float* __restrict__ 
 __global__ void __launch_bounds__(256) horseshoe_finish_kernel(const float* __restrict__ Q, int npts, int ld, int P,
                                                                int64_t N, const float* __restrict__ part_gb,
                                                                int splits, int ldg, const double* __restrict__ part_rr,
-                                                               int ld_rr, int mtiles, double* __restrict__ PE,
-                                                               float* __restrict__ G, const int32_t* pending) {
+                                                               int ld_rr, int mtiles, int noncentred,
+                                                               double* __restrict__ PE, float* __restrict__ G,
+                                                               const int32_t* pending) {
   if (pending && *pending == 0) return;
   __shared__ double red[16];
   const int c = blockIdx.x, tid = threadIdx.x;
   Group<256> g{tid};
   const float* z = Q + (size_t)c * ld;
   float* gz = G + (size_t)c * ld;
-  const float lsig = z[2 * P], ltau = z[2 * P + 1];
+  const int i_sig = noncentred ? P : 2 * P, i_tau = i_sig + 1;
+  const float lsig = z[i_sig], ltau = z[i_tau];
   const float inv_sig2 = expf(-2.0f * lsig);
   double rrd = 0.0;  // this thread's row tiles (at most a few), then a float-float pair
   for (int t = tid; t < mtiles; t += 256) rrd += part_rr[(size_t)t * ld_rr + c];
@@ -334,18 +346,30 @@ __global__ void __launch_bounds__(256) horseshoe_finish_kernel(const float* __re
   const FF rr_ff{rr_hi, (float)(rrd - (double)rr_hi)};
   Comp32 lp{0.0f, 0.0f}, gt{0.0f, 0.0f};
   for (int d = tid; d < P; d += 256) {
-    const float b = z[d], l = z[P + d];
     float gb = 0.0f;
     for (int k = 0; k < splits; ++k) gb += part_gb[((size_t)k * npts + c) * ldg + d];
-    const float inv_s2 = expf(-2.0f * (ltau + l));
-    const float b2s = b * b * inv_s2;
+    const float gx = gb * inv_sig2;  // (X^T R)_d / sigma^2
+    const float l = noncentred ? z[d] : z[P + d];
     const float e2 = expf(-2.0f * fabsf(l));
     const float log1p_lam2 = 2.0f * fmaxf(l, 0.0f) + log1pf(e2);
     const float hc = (l >= 0.0f) ? 2.0f / (1.0f + e2) : 2.0f * e2 / (1.0f + e2);  // 2 lam^2 / (1 + lam^2)
-    gz[d] = b * inv_s2 - gb * inv_sig2;
-    gz[P + d] = hc - b2s;
-    lp.add(-0.5f * b2s - log1p_lam2);
-    gt.add(1.0f - b2s);
+    if (noncentred) {
+      const float eta = z[P + 2 + d];
+      const float scale = expf(ltau + l);  // tau lambda_d
+      const float bg = scale * eta * gx;   // beta_d g_d
+      gz[P + 2 + d] = eta - scale * gx;
+      gz[d] = hc - 1.0f - bg;
+      lp.add(-0.5f * eta * eta - log1p_lam2 + l);
+      gt.add(-bg);
+    } else {
+      const float b = z[d];
+      const float inv_s2 = expf(-2.0f * (ltau + l));
+      const float b2s = b * b * inv_s2;
+      gz[d] = b * inv_s2 - gx;
+      gz[P + d] = hc - b2s;
+      lp.add(-0.5f * b2s - log1p_lam2);
+      gt.add(1.0f - b2s);
+    }
   }
   FF flp = comp_ff(lp), fgt = comp_ff(gt);
   g.sum2ff(flp, fgt, red);
@@ -353,13 +377,14 @@ __global__ void __launch_bounds__(256) horseshoe_finish_kernel(const float* __re
   if (tid == 0) {
     const double RR = ff_value(frr), dlsig = lsig, dltau = ltau;
     const double sig = exp(dlsig), tau = exp(dltau), inv_s2 = exp(-2.0 * dlsig);
-    double total = ff_value(flp) + (double)P * (LOG_2 - LOG_PI - 0.5 * LOG_2PI - dltau);
+    // per coordinate: Normal(beta; 0, tau lambda) or Normal(unscaled; 0, 1), HalfCauchy(lambda; 1)
+    double total = ff_value(flp) + (double)P * (LOG_2 - LOG_PI - 0.5 * LOG_2PI - (noncentred ? 0.0 : dltau));
     total += -0.5 * sig * sig - 0.5 * LOG_2PI + LOG_2 + dlsig;  // HalfNormal(sigma; 1) + log-det
     total += -LOG_PI - log1p(tau * tau) + LOG_2 + dltau;        // HalfCauchy(tau; 1) + log-det
     total += -0.5 * RR * inv_s2 - (double)N * dlsig - 0.5 * (double)N * LOG_2PI;
     PE[c] = -total;
-    gz[2 * P] = (float)(sig * sig - 1.0 - RR * inv_s2 + (double)N);
-    gz[2 * P + 1] = (float)(ff_value(fgt) + 2.0 * tau * tau / (1.0 + tau * tau) - 1.0);
+    gz[i_sig] = (float)(sig * sig - 1.0 - RR * inv_s2 + (double)N);
+    gz[i_tau] = (float)(ff_value(fgt) + 2.0 * tau * tau / (1.0 + tau * tau) - 1.0);
   }
 }
 
@@ -471,7 +496,8 @@ cudaError_t launch_potential(ModelDev& m, const float* Q, int npts, double* PE, 
       const int mt = (M + HS_BM - 1) / HS_BM;
       // beta^T for the chains' query points
       dim3 gp((cp + 31) / 32, (pp + 31) / 32);
-      hs_pack_kernel<<<gp, 256, 0, st>>>(Q, ld, npts, P, m.hs_bt, cp, pp, pending);
+      const int nc = m.hyper[0] != 0.0;
+      hs_pack_kernel<<<gp, 256, 0, st>>>(Q, ld, npts, P, nc, m.hs_bt, cp, pp, pending);
       // R[row][c] = y[row] - sum_p X[row][p] beta_c[p]
       dim3 g1((npts + HS_BN - 1) / HS_BN, mt, 1);
       hs_sgemm_nn_kernel<<<g1, 256, 0, st>>>(m.hs_xt, pad4(M), m.hs_bt, cp, M, npts, P, P, m.resid, cp, 0, m.y,
@@ -482,7 +508,7 @@ cudaError_t launch_potential(ModelDev& m, const float* Q, int npts, double* PE, 
       hs_sgemm_nn_kernel<<<g2, 256, 0, st>>>(m.resid, cp, m.hs_xp, pp, npts, P, M, kps, m.part_gb, pp,
                                              (int64_t)npts * pp, nullptr, nullptr, 0, pending);
       horseshoe_finish_kernel<<<npts, 256, 0, st>>>(Q, npts, ld, P, m.n, m.part_gb, HS_SPLITS, pp, m.part_rr, cp,
-                                                    mt, PE, G, pending);
+                                                    mt, nc, PE, G, pending);
       break;
     }
     case 4:

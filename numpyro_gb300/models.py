@@ -16,9 +16,11 @@ Models written as numpyro programs (for reference):
       y_j ~ Normal(theta_j, sigma_j)
   LogisticRegression (examples/covtype.py:66-71)
       coefs ~ Normal(0, prior_scale)^D; obs ~ Bernoulli(logits = X coefs)
-  HorseshoeRegression (centred, Gaussian likelihood)
+  HorseshoeRegression (Gaussian likelihood)
       tau ~ HalfCauchy(1); lambdas ~ HalfCauchy(1)^P; beta ~ Normal(0, tau*lambdas)
       sigma ~ HalfNormal(1); y ~ Normal(X beta, sigma)
+      noncentered=True (examples/horseshoe_regression.py:33-49): unscaled_betas ~ Normal(0, 1)^P,
+      beta = tau * lambdas * unscaled_betas (deterministic)
   StochasticVolatility (examples/stochastic_volatility.py:58-66)
       s ~ Exponential(s_rate); nu ~ Exponential(nu_rate)
       h ~ GaussianRandomWalk(scale=s, num_steps=T); r_t ~ StudentT(nu, 0, exp(h_t))
@@ -155,12 +157,23 @@ class LogisticRegression(Model):
 class HorseshoeRegression(Model):
     family = _lib.FAMILY_HORSESHOE
 
-    def __init__(self, X, y):
+    def __init__(self, X, y, noncentered=False):
         self.X = np.ascontiguousarray(np.asarray(X, np.float32))
         self.y = np.ascontiguousarray(np.asarray(y, np.float32).ravel())
+        self.noncentered = bool(noncentered)
         P = self.X.shape[1]
-        self.sites = (Site("beta", P, False), Site("lambdas", P, True), Site("sigma", 1, True),
-                      Site("tau", 1, True))
+        if self.noncentered:
+            self.sites = (Site("lambdas", P, True), Site("sigma", 1, True), Site("tau", 1, True),
+                          Site("unscaled_betas", P, False))
+        else:
+            self.sites = (Site("beta", P, False), Site("lambdas", P, True), Site("sigma", 1, True),
+                          Site("tau", 1, True))
+
+    def postprocess(self, z):
+        out = super().postprocess(z)
+        if self.noncentered:
+            out["beta"] = out["tau"] * out["lambdas"] * out["unscaled_betas"]
+        return out
 
     def descriptor(self):
         d = _lib.ModelDesc()
@@ -170,6 +183,7 @@ class HorseshoeRegression(Model):
         d.p = self.X.shape[1]
         d.x = _fp(self.X)
         d.y = _fp(self.y)
+        d.hyper[0] = 1.0 if self.noncentered else 0.0
         return d, (self.X, self.y)
 
 

@@ -136,6 +136,39 @@ def horseshoe_grad(z, X, y):
     return g
 
 
+# Non-centred horseshoe (examples/horseshoe_regression.py:33-49 with the HalfNormal(1) noise
+# scale): sorted sites lambdas, sigma, tau, unscaled_betas -> z = [log lam(P), log sig, log tau, eta(P)],
+# beta = tau * lam * eta, eta ~ Normal(0, 1).
+def horseshoe_nc_potential(z, X, y):
+    z = np.asarray(z, np.float64)
+    P = X.shape[1]
+    llam, lsig, ltau, eta = z[:P], z[P], z[P + 1], z[P + 2:]
+    lam, sig, tau = np.exp(llam), math.exp(lsig), math.exp(ltau)
+    beta = tau * lam * eta
+    lp = np.sum(_normal_lp(eta, 0.0, 1.0))
+    lp += np.sum(_halfcauchy_lp(lam, 1.0)) + np.sum(llam)
+    lp += _normal_lp(sig, 0.0, 1.0) + LOG_2 + lsig
+    lp += _halfcauchy_lp(tau, 1.0) + ltau
+    lp += np.sum(_normal_lp(y - X @ beta, 0.0, sig))
+    return -float(lp)
+
+
+def horseshoe_nc_grad(z, X, y):
+    z = np.asarray(z, np.float64)
+    N, P = X.shape
+    llam, lsig, ltau, eta = z[:P], z[P], z[P + 1], z[P + 2:]
+    lam, sig, tau = np.exp(llam), math.exp(lsig), math.exp(ltau)
+    beta = tau * lam * eta
+    resid = y - X @ beta
+    gx = X.T @ resid / sig ** 2                      # -dU_lik/dbeta
+    g = np.empty(2 * P + 2)
+    g[P + 2:] = eta - tau * lam * gx
+    g[:P] = -beta * gx + 2.0 * lam ** 2 / (1.0 + lam ** 2) - 1.0
+    g[P] = sig ** 2 - 1.0 - np.sum(resid ** 2) / sig ** 2 + N
+    g[P + 1] = -np.sum(beta * gx) + 2.0 * tau ** 2 / (1.0 + tau ** 2) - 1.0
+    return g
+
+
 # --------------------------------------------------------------------------
 # Stochastic volatility (examples/stochastic_volatility.py:58-66 with the
 # Exponential(10) scale prior):  s ~ Exponential(10); nu ~ Exponential(0.1)
@@ -227,6 +260,7 @@ FAMILIES = {
     "hier_nc": (hier_nc_potential, hier_nc_grad),
     "logreg": (logreg_potential, logreg_grad),
     "horseshoe": (horseshoe_potential, horseshoe_grad),
+    "horseshoe_nc": (horseshoe_nc_potential, horseshoe_nc_grad),
     "sv": (sv_potential, sv_grad),
     "sv_nc": (sv_nc_potential, sv_nc_grad),
 }

@@ -17,6 +17,8 @@ def family_cases(small=True):
     Xh, yh, _ = datasets.horseshoe_data(seed=2, n=200, p=50, nonzero=5)
     out.append(("horseshoe", models.HorseshoeRegression(Xh, yh),
                 PR.make_potential("horseshoe", Xh.astype(np.float64), yh.astype(np.float64))))
+    out.append(("horseshoe_nc", models.HorseshoeRegression(Xh, yh, noncentered=True),
+                PR.make_potential("horseshoe_nc", Xh.astype(np.float64), yh.astype(np.float64))))
     r, _ = datasets.sv_returns(seed=3, T=300)
     out.append(("sv", models.StochasticVolatility(r), PR.make_potential("sv", r.astype(np.float64))))
     r2, _ = datasets.sv_returns(seed=4, T=1000)
@@ -44,6 +46,14 @@ def typical_points(name, model, rng, C):
         return z.astype(np.float32)
     if name == "logreg":
         return (0.3 * rng.standard_normal((C, D))).astype(np.float32)
+    if name == "horseshoe_nc":
+        P = (D - 2) // 2
+        z = np.empty((C, D))
+        z[:, :P] = rng.standard_normal((C, P))
+        z[:, P] = 0.3 * rng.standard_normal(C)
+        z[:, P + 1] = -2.0 + 0.3 * rng.standard_normal(C)
+        z[:, P + 2:] = rng.standard_normal((C, P))
+        return z.astype(np.float32)
     if name == "horseshoe":
         P = (D - 2) // 2
         z = np.empty((C, D))

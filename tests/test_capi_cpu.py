@@ -79,6 +79,10 @@ def test_model_layout_sorted_sites():
     assert m.latent_dim == 8
     out = m.postprocess(np.zeros(8))
     assert out["sigma"].item() == 1.0 and out["beta"].shape == (3,)
+    hn = models.HorseshoeRegression(np.zeros((5, 3)), np.zeros(5), noncentered=True)
+    assert [s.name for s in hn.sites] == ["lambdas", "sigma", "tau", "unscaled_betas"]
+    zz = np.concatenate([np.zeros(3), [0.0, np.log(2.0)], [1.0, 2.0, 3.0]])
+    np.testing.assert_allclose(hn.postprocess(zz)["beta"], [2.0, 4.0, 6.0])
     sv = models.StochasticVolatility(np.zeros(10))
     assert [s.name for s in sv.sites] == ["h", "nu", "s"] and sv.latent_dim == 12
     nc = models.StochasticVolatility(np.zeros(10), noncentered=True)

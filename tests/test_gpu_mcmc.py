@@ -92,11 +92,11 @@ def test_hmc_kernel_runs_and_adapts():
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("name", ["horseshoe", "sv"])
+@pytest.mark.parametrize("name", ["horseshoe", "horseshoe_nc", "sv"])
 def test_large_latent_families_run(name):
-    if name == "horseshoe":
+    if name.startswith("horseshoe"):
         X, yh, beta = datasets.horseshoe_data(seed=1, n=300, p=60, nonzero=4)
-        model = models.HorseshoeRegression(X, yh)
+        model = models.HorseshoeRegression(X, yh, noncentered=name.endswith("_nc"))
     else:
         r, _ = datasets.sv_returns(seed=1, T=600)
         model = models.StochasticVolatility(r)
