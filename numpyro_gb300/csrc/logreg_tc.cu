@@ -6,18 +6,25 @@
 //  binary_cross_entropy_with_logits distributions/util.py:317-320, Normal prior
 //  continuous.py:2975-2989, potential_energy infer/util.py:333-358.)
 //
-// One CTA owns 128 chains and a strided set of 128-row tiles of X:
-//   warp 0      TMA producer: X tile [128 rows x 64 feat] bf16, 128B swizzle, 4-stage ring
-//   warp 1      MMA issuer:  GEMM1  L[128 rows x 128 chains] = X_tile . (b_hi + b_mid + b_lo)^T
+// Sign-flipped rows.  With s_n = 1 - 2 y_n and X'_n = s_n X_n (exact in bf16):
+//   softplus(l_n) - y_n l_n = softplus(l'_n) = l'_n/2 + |l'_n|/2 + log(1 + e^{-|l'_n|}),  l' = X' b
+//   sum_n (sigmoid(l_n) - y_n) X_n = sum_n sigmoid(l'_n) X'_n
+// so the kernel never reads y: it streams X' and the linear part sum_n l'_n / 2 = (X'^T 1 / 2) . b
+// is added per chain from a vector computed once.
+//
+// One CTA owns 128 chains and a strided set of 128-row tiles of X':
+//   warp 0      TMA producer: X' tile [128 rows x 64 feat] bf16, 128B swizzle, 4-stage ring
+//   warp 1      MMA issuer:  GEMM1  H[128 chains x 128 rows] = (b_hi + b_mid + b_lo)/2 . X'_tile^T
 //                            (three K=64 BF16 products accumulate in FP32 in TMEM, so the
 //                            FP32 coefficients are represented exactly: "bf16x3"),
-//                            GEMM2  G[128 chains x 64 feat] += E^T . X_tile  (E = sigmoid(L) - y)
-//   warps 2..17 epilogue (4 per TMEM lane quadrant, 32 chains each): tcgen05.ld of L
-//               (software-pipelined), sigmoid/softplus with one ex2, one lg2 and one
-//               tanh per logit (special-function bound), E as bf16 into shared memory; the
-//               log-likelihood accumulates per thread in FP32 registers across tiles and is
-//               reduced once per CTA (lane butterfly, then FP64 across the lane quadrants).
-// L is double-buffered in TMEM (2 x 128 columns) so GEMM1 of tile t+1 overlaps the
+//                            GEMM2  G[128 chains x 64 feat] += E . X'_tile  (E = sigmoid(l'))
+//   warps 2..17 epilogue: TMEM lanes are chains, columns rows; 4 warps per lane quadrant split
+//               the 128 rows.  Per logit one ex2 and one tanh; log(1 + e^{-|l'|}) is taken as one
+//               lg2 of the product of 8 rows' factors (2.125 special-function ops per logit).
+//               E goes to shared memory as bf16 in the K-major layout GEMM2 reads.  Each thread
+//               accumulates its chain's log-likelihood over its rows; the four row quarters are
+//               combined once per CTA in FP64.
+// H is double-buffered in TMEM (2 x 128 columns) so GEMM1 of tile t+1 overlaps the
 // epilogue of tile t; G lives in TMEM for the whole launch (64 columns).
 // The design matrix must be exactly representable in bf16 (checked on the host).
 // Every mbarrier wait is bounded; on a timeout the CTA records an error, drains its
@@ -50,7 +57,6 @@ constexpr int OFF_MISC = OFF_S + 2 * S_TILE;
 constexpr int NUM_BARS = 2 * STAGES + 2 + 2 + 2 + 2 + 1;
 constexpr int SMEM_BYTES = OFF_MISC + 256 + BN * 8 + 1024;  // + alignment slack
 constexpr int EPI_WARPS = 16;             // epilogue warps: 4 per TMEM lane quadrant
-constexpr int CW = BN * 4 / EPI_WARPS;    // chains per epilogue warp
 constexpr int GCOLS = BK * 4 / EPI_WARPS; // gradient columns read back per epilogue warp
 constexpr int NUM_THREADS = 32 * (2 + EPI_WARPS);
 constexpr uint32_t TMEM_COLS = 512;
@@ -181,89 +187,57 @@ __device__ __forceinline__ float tanh_approx(float x) {
   return y;
 }
 
-// One tile of the epilogue for one warp: 32 rows (this lane's row) x 64 chains.
-// The accumulator holds h = l/2 (the coefficients enter GEMM1 halved, an exact scaling).
-//   sigmoid(l) - y = tanh(h)/2 + (1/2 - y)
-//   softplus(l)   = l/2 + |h| + log(1 + exp(-|l|))
-// so the per-logit log-likelihood work is |h| + log(1 + exp(-2|h|)); the linear parts
-// sum_r l_r/2 and sum_r y_r l_r are added per chain as (X^T 1 / 2 - X^T y) . b.
-// MASK zeroes rows past the end of the data.
-// The warp covers CW chains starting at column col0 of the tile (CW a multiple of 16).
-template <bool MASK, int CW>
-__device__ __forceinline__ void epilogue_tile(uint32_t taddr, float yv, float vmask, uint8_t* sdst, int row, int col0,
-                                              float (&acc)[CW], uint32_t acc_empty_bar, int lane) {
-  constexpr int NCH = CW / 16;
-  const float NEG_2LOG2E = -2.8853900817779268f, LN2 = 0.6931471805599453f;
-  // 1/2 - y; zero for rows past the data (their logits are zero and tanh(0) = 0)
-  const float c05 = (MASK && vmask == 0.0f) ? 0.0f : 0.5f - yv;
+// One tile of the epilogue for one warp: its lane's chain x 32 rows (TMEM columns at taddr).
+// TMEM holds h = l'/2 (the coefficients enter GEMM1 halved, an exact scaling).  Per row:
+//   E = sigmoid(l') = tanh(h)/2 + 1/2                      -> bf16, K-major tile for GEMM2
+//   softplus(l') - l'/2 = |h| + log(1 + e^{-2|h|})          -> |h| summed, the logs taken as
+//                                                            one log2 per product of 8 rows
+// With MASK, rows r >= nvalid lie past the end of the data: they are left out of the
+// log-likelihood (their X' rows are zero, so E needs no mask).
+// E is written to erow: this chain's 128-byte row of the swizzled K-major tile, 16-byte chunk
+// chunk0 + g for rows 8g..8g+7, XOR-swizzled with the chain index cx = chain & 7.
+template <bool MASK>
+__device__ __forceinline__ void epilogue_tile(uint32_t taddr, uint8_t* erow, int chunk0, int cx, int nvalid,
+                                              float& sabs, float& slg, uint32_t acc_empty_bar, int lane) {
+  const float NEG_2LOG2E = -2.8853900817779268f;
   uint32_t v[2][16];
   tmem_ld16u(taddr, v[0]);
+  tmem_ld16u(taddr + 16, v[1]);
   tmem_wait16(v[0]);
-  if (NCH == 1) {  // every column of this accumulator has been read: release it to the MMA warp
-    tc_fence_before();
-    __syncwarp();
-    if (lane == 0) bar_arrive(acc_empty_bar);
-  }
+  tmem_wait16(v[1]);
+  // every column of this warp's share has been read: release the accumulator to the MMA warp
+  tc_fence_before();
+  __syncwarp();
+  if (lane == 0) bar_arrive(acc_empty_bar);
+  float ta = 0.0f, tl = 0.0f;
 #pragma unroll
-  for (int j = 0; j < NCH; ++j) {
-    if (j + 1 < NCH) tmem_ld16u(taddr + 16 * (j + 1), v[(j + 1) & 1]);
-    uint32_t pk[8];
+  for (int g8 = 0; g8 < 4; ++g8) {
+    float prod = 1.0f;
+    uint32_t pk[4];
 #pragma unroll
-    for (int e = 0; e < 16; e += 2) {
+    for (int e = 0; e < 8; e += 2) {
       float ev[2];
 #pragma unroll
-      for (int h = 0; h < 2; ++h) {
-        const float hl = __uint_as_float(v[j & 1][e + h]);
-        const float t = ex2_approx(fabsf(hl) * NEG_2LOG2E);  // exp(-|l|)
-        const float lg = lg2_approx(1.0f + t);               // log2(1 + exp(-|l|))
-        float llv = fmaf(LN2, lg, fabsf(hl));
-        if (MASK) llv *= vmask;
-        acc[16 * j + e + h] += llv;
-        // E = tanh(l/2)/2 + (1/2 - y) in FP32, rounded once to bf16 (rows past the data give 0)
-        ev[h] = fmaf(0.5f, tanh_approx(hl), c05);
+      for (int hh = 0; hh < 2; ++hh) {
+        const int r = 8 * g8 + e + hh;
+        const float h = __uint_as_float(v[r >> 4][r & 15]);
+        const float t = ex2_approx(fabsf(h) * NEG_2LOG2E);  // e^{-|l'|}
+        if (!MASK || r < nvalid) {
+          ta += fabsf(h);
+          prod *= 1.0f + t;
+        }
+        ev[hh] = fmaf(0.5f, tanh_approx(h), 0.5f);
       }
       pk[e >> 1] = pack_bf16(ev[0], ev[1]);
     }
-    // E[row][col0 + 16 j + 0..15]: two 16-byte chunks of the swizzled MN-major tile
-#pragma unroll
-    for (int hh = 0; hh < 2; ++hh) {
-      const int c8 = (col0 >> 3) + 2 * j + hh;  // 8-chain chunk index in [0, 16)
-      uint4 w = make_uint4(pk[4 * hh], pk[4 * hh + 1], pk[4 * hh + 2], pk[4 * hh + 3]);
-      *reinterpret_cast<uint4*>(sdst + (c8 >> 3) * 1024 + (((c8 & 7) ^ (row & 7)) << 4)) = w;
-    }
-    if (j + 1 < NCH) {
-      tmem_wait16(v[(j + 1) & 1]);
-      if (j + 2 == NCH) {  // every column of this accumulator has been read: release it to the MMA warp
-        tc_fence_before();
-        __syncwarp();
-        if (lane == 0) bar_arrive(acc_empty_bar);
-      }
-    }
+    tl += lg2_approx(prod);
+    *reinterpret_cast<uint4*>(erow + (((chunk0 + g8) ^ cx) << 4)) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
   }
-}
-
-// One halving step of the transposed butterfly: lanes with bit `off` set keep the upper half.
-template <int N>
-__device__ __forceinline__ void butterfly_step(const float* a, float* b, int lane, int off) {
-  const bool up = lane & off;
-#pragma unroll
-  for (int i = 0; i < N / 2; ++i)
-    b[i] = (up ? a[N / 2 + i] : a[i]) + __shfl_xor_sync(0xffffffffu, up ? a[i] : a[N / 2 + i], off);
-}
-// Transposed butterfly over the 32 lanes of N values: lane l returns the lane-sums of
-// values (N/32) l + i, i < N/32.
-template <int N>
-__device__ __forceinline__ void warp_transpose_sum(const float (&a)[N], float (&out)[N / 32], int lane) {
-  float b[N / 2], c[N / 4], d[N / 8], e[N / 16];
-  butterfly_step<N>(a, b, lane, 16);
-  butterfly_step<N / 2>(b, c, lane, 8);
-  butterfly_step<N / 4>(c, d, lane, 4);
-  butterfly_step<N / 8>(d, e, lane, 2);
-  butterfly_step<N / 16>(e, out, lane, 1);
+  sabs += ta;
+  slg += tl;
 }
 
 struct Params {
-  const float* y;
   int64_t n;
   const __nv_bfloat16* bsplit;  // [chain_blocks*128][3][64]
   int npts;
@@ -353,8 +327,8 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) logreg_tc_kernel(const __grid_
   } else if (warp == 1) {
     // ------------------------------------------------------------ MMA issuer
     if (lane == 0) {
-      constexpr uint32_t ID1 = idesc(BM, BN, 0, 0);  // L = X . B^T, both K-major
-      constexpr uint32_t ID2 = idesc(BN, BK, 1, 1);  // G = E^T . X, both MN-major
+      constexpr uint32_t ID1 = idesc(BN, BM, 0, 0);  // H = B . X'^T: chains x rows, both K-major
+      constexpr uint32_t ID2 = idesc(BN, BK, 0, 1);  // G = E . X': E K-major, X' MN-major
       const uint32_t xb = smem_u32(smem + OFF_X), bb = smem_u32(smem + OFF_B), sb = smem_u32(smem + OFF_S);
       bool ok = true;
       int committed_gemm2 = -1;
@@ -371,8 +345,8 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) logreg_tc_kernel(const __grid_
           for (int k = 0; k < NSPLIT; ++k) {
 #pragma unroll
             for (int kk = 0; kk < BK / 16; ++kk) {
-              uint64_t a = sdesc(xb + s * X_TILE + kk * 32, 16, 1024);
-              uint64_t bd = sdesc(bb + k * B_TILE + kk * 32, 16, 1024);
+              uint64_t a = sdesc(bb + k * B_TILE + kk * 32, 16, 1024);
+              uint64_t bd = sdesc(xb + s * X_TILE + kk * 32, 16, 1024);
               mma_bf16(d, a, bd, ID1, first ? 0u : 1u);
               first = 0;
             }
@@ -386,8 +360,8 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) logreg_tc_kernel(const __grid_
           tc_fence_after();
 #pragma unroll
           for (int kk = 0; kk < BM / 16; ++kk) {
-            // A = E[b]: MN-major, 64-chain atoms 1024 B apart (LBO), 8-row groups 2048 B apart (SBO)
-            uint64_t a = sdesc(sb + b * S_TILE + kk * 4096, 1024, 2048);
+            // A = E[b]: K-major [128 chains][128 rows] as two 64-row swizzled halves of 16 KB
+            uint64_t a = sdesc(sb + b * S_TILE + (kk >> 2) * (BN * 64 * 2) + (kk & 3) * 32, 16, 1024);
             // B = X tile: MN-major (features contiguous), 8-row groups 1024 B apart (SBO)
             uint64_t bd = sdesc(xb + s * X_TILE + kk * 2048, 1024, 1024);
             mma_bf16(tmem + ACC2_COL, a, bd, ID2, (j > 0 || kk > 0) ? 1u : 0u);
@@ -406,57 +380,45 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) logreg_tc_kernel(const __grid_
   } else {
     // ------------------------------------------------------------ epilogue (warps 2..17)
     const int ew = warp - 2;
-    const int q = warp & 3;         // TMEM lane quadrant this warp may access
-    const int ch = ew >> 2;         // column group: chains [CW*ch, CW*ch+CW)
-    const int row = q * 32 + lane;  // row within the tile
-    const int col0 = ch * CW;       // first chain (tile column) of this warp
-    // log-likelihood partials of the warp's CW chains for this lane's row slot, over all tiles
-    float acc[CW];
-#pragma unroll
-    for (int k = 0; k < CW; ++k) acc[k] = 0.0f;
-    const uint32_t tl = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)col0;
+    const int q = warp & 3;          // TMEM lane quadrant this warp may access: chains 32q..32q+31
+    const int rq = ew >> 2;          // row quarter of each tile: rows 32 rq .. 32 rq + 31
+    const int c = q * 32 + lane;     // this thread's chain within the CTA
+    const uint32_t tl = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(rq * 32);
+    // this chain's row of the E tile (K-major, rows 64 (rq / 2) .. of the tile)
+    uint8_t* erow0 = smem + OFF_S + (rq >> 1) * (BN * 64 * 2) + (c >> 3) * 1024 + (c & 7) * 128;
+    Comp32 ll{0.0f, 0.0f};  // log-likelihood of this chain over this thread's rows, all tiles
     bool ok = true;
-    float y_next = 0.0f;
-    if (my_tiles > 0 && (int64_t)rg * BM + row < P.n) y_next = P.y[(int64_t)rg * BM + row];
     for (int i = 0; i < my_tiles && ok; ++i) {
       const int b = i & 1;
       const int64_t row0 = ((int64_t)rg + (int64_t)i * P.row_groups) * BM;
-      const float yv = y_next;
-      if (i + 1 < my_tiles) {
-        const int64_t gn = row0 + (int64_t)P.row_groups * BM + row;
-        y_next = gn < P.n ? P.y[gn] : 0.0f;
-      }
       ok = bar_wait(bar(B_ACCF + b), (i >> 1) & 1, abort_flag, P.err);
       if (ok && i >= 2) ok = bar_wait(bar(B_SE + b), ((i >> 1) - 1) & 1, abort_flag, P.err);
       if (!ok) break;
       tc_fence_after();
-      uint8_t* sdst = smem + OFF_S + b * S_TILE + (row >> 3) * 2048 + (row & 7) * 128;
-      if (row0 + BM <= P.n)
-        epilogue_tile<false, CW>(tl + (uint32_t)(b * BN), yv, 1.0f, sdst, row, col0, acc, bar(B_ACCE + b), lane);
+      float sabs = 0.0f, slg = 0.0f;
+      const int64_t nleft = P.n - (row0 + rq * 32);
+      if (nleft >= 32)
+        epilogue_tile<false>(tl + (uint32_t)(b * BM), erow0 + b * S_TILE, (rq & 1) * 4, c & 7, 32, sabs, slg,
+                             bar(B_ACCE + b), lane);
       else
-        epilogue_tile<true, CW>(tl + (uint32_t)(b * BN), yv, (row0 + row < P.n) ? 1.0f : 0.0f, sdst, row, col0,
-                                acc, bar(B_ACCE + b), lane);
+        epilogue_tile<true>(tl + (uint32_t)(b * BM), erow0 + b * S_TILE, (rq & 1) * 4, c & 7,
+                            nleft > 0 ? (int)nleft : 0, sabs, slg, bar(B_ACCE + b), lane);
+      ll.add(fmaf(0.6931471805599453f, slg, sabs));
       fence_proxy_async();
       __syncwarp();
       if (lane == 0) bar_arrive(bar(B_SF + b));
     }
-    // per-chain sums over the CTA's rows: butterfly over lanes, then the four lane quadrants
-    if (ok) {
-      float s[CW / 32];
-      warp_transpose_sum<CW>(acc, s, lane);
-#pragma unroll
-      for (int k = 0; k < CW / 32; ++k) atomicAdd(&ll_smem[col0 + (CW / 32) * lane + k], (double)s[k]);
-    }
+    // per-chain sums over the CTA's rows: the four row quarters meet in shared memory (FP64)
+    if (ok) atomicAdd(&ll_smem[c], comp_total(ll));
     // gradient partials: G (lanes = chains, 64 feature columns)
     if (ok) ok = bar_wait(bar(B_DONE), 0, abort_flag, P.err);
     if (ok) {
       tc_fence_after();
-      const int c = q * 32 + lane;
       const int gc = cb * BN + c;
 #pragma unroll
       for (int j = 0; j < GCOLS / 16; ++j) {
         float v[16];
-        const int colb = ch * GCOLS + j * 16;
+        const int colb = rq * GCOLS + j * 16;
         tmem_ld16(tmem + ((uint32_t)(q * 32) << 16) + ACC2_COL + (uint32_t)colb, v);
         tmem_wait_ld();
         if (gc < P.npts) {
@@ -500,20 +462,22 @@ __global__ void split_coefs_kernel(const float* __restrict__ Q, int npts, int ld
   o[2 * BK] = lo;
 }
 
-__global__ void to_bf16_kernel(const float* __restrict__ x, int64_t n, int p, __nv_bfloat16* __restrict__ out,
-                               int* inexact) {
+// X'[r] = (1 - 2 y_r) X[r] in bf16, rows padded to 64 features; flags values bf16 cannot hold
+__global__ void to_bf16_kernel(const float* __restrict__ x, const float* __restrict__ y, int64_t n, int p,
+                               __nv_bfloat16* __restrict__ out, int* inexact) {
   int64_t total = n * BK;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
     int64_t r = i / BK;
     int d = (int)(i % BK);
-    float v = (d < p) ? x[r * p + d] : 0.0f;
+    const float sgn = (y[r] > 0.5f) ? -1.0f : 1.0f;
+    float v = (d < p) ? sgn * x[r * p + d] : 0.0f;
     __nv_bfloat16 h = __float2bfloat16_rn(v);
     if (__bfloat162float(h) != v) atomicExch(inexact, 1);
     out[i] = h;
   }
 }
 
-// lin[d] = sum_r (1/2 - y_r) X_rd in FP64 (the linear part of the log-likelihood)
+// lin[d] = sum_r (1/2 - y_r) X_rd = (X'^T 1 / 2)_d in FP64 (the linear part of the log-likelihood)
 __global__ void linear_term_kernel(const float* __restrict__ x, const float* __restrict__ y, int64_t n, int p,
                                    double* __restrict__ lin) {
   __shared__ double part[4][64];
@@ -574,7 +538,7 @@ cudaError_t logreg_tc_prepare(ModelDev& m, int points) {
     if (e == cudaSuccess) e = cudaMalloc(&s->err, sizeof(int) * 2);
     if (e != cudaSuccess) return e;
     cudaMemset(s->err, 0, sizeof(int) * 2);
-    tc::to_bf16_kernel<<<1024, 256>>>(m.x, m.n, m.p, s->xb, s->err + 1);
+    tc::to_bf16_kernel<<<1024, 256>>>(m.x, m.y, m.n, m.p, s->xb, s->err + 1);
     int inexact = 0;
     e = cudaMemcpy(&inexact, s->err + 1, sizeof(int), cudaMemcpyDeviceToHost);
     if (e != cudaSuccess) return e;
@@ -643,7 +607,7 @@ cudaError_t logreg_tc_launch(ModelDev& m, const float* Q, int npts, double* PE, 
   if (rg > m.row_groups) rg = m.row_groups;  // partial buffers are sized for m.row_groups
   int npad = blocks * tc::BN;
   tc::split_coefs_kernel<<<(npad * tc::BK + 255) / 256, 256, 0, st>>>(Q, npts, m.D, m.p, npad, s->bsplit, pending);
-  tc::Params P{m.y, m.n, s->bsplit, npts, rg, m.part_g, m.part_ll, s->err, pending};
+  tc::Params P{m.n, s->bsplit, npts, rg, m.part_g, m.part_ll, s->err, pending};
   tc::logreg_tc_kernel<<<dim3(blocks, rg), tc::NUM_THREADS, tc::SMEM_BYTES, st>>>(s->tmap, P);
   logreg_finish_launch(Q, npts, m.D, m.p, rg, m.part_g, m.part_ll, s->lin, m.hyper[0], PE, G, pending, st);
   return cudaGetLastError();
