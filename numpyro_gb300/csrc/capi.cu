@@ -9,6 +9,7 @@
 #include <cmath>
 #include <cstdio>
 #include <algorithm>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -43,6 +44,11 @@ struct gbn_handle_s {
   gbn_stats stats{};
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   std::vector<void*> allocs;
+  // CUDA graph of one batch of ticks (advance + potential launches), replayed by tick_loop
+  int use_graphs = 1;
+  cudaStream_t cap_stream = nullptr;
+  cudaGraphExec_t tick_graph = nullptr;
+  void* graph_scratch = nullptr;  // potential scratch the graph was captured with
 };
 
 static thread_local std::string g_last_error;
@@ -157,6 +163,8 @@ int gbn_destroy(gbn_handle h) {
   if (h->h_counters) cudaFreeHost(h->h_counters);
   if (h->ev0) cudaEventDestroy(h->ev0);
   if (h->ev1) cudaEventDestroy(h->ev1);
+  if (h->tick_graph) cudaGraphExecDestroy(h->tick_graph);
+  if (h->cap_stream) cudaStreamDestroy(h->cap_stream);
   delete h;
   return GBN_OK;
 }
@@ -317,6 +325,11 @@ int gbn_create(gbn_handle* out, const gbn_model_desc* md, const gbn_config* cfg)
   if (ce == cudaSuccess) ce = cudaMallocHost((void**)&h->h_counters, sizeof(int32_t) * 8);
   if (ce == cudaSuccess) ce = cudaEventCreate(&h->ev0);
   if (ce == cudaSuccess) ce = cudaEventCreate(&h->ev1);
+  if (ce == cudaSuccess) ce = cudaStreamCreateWithFlags(&h->cap_stream, cudaStreamNonBlocking);
+  {
+    const char* g = getenv("GBN_CUDA_GRAPHS");  // "0" launches every tick directly
+    h->use_graphs = !(g && g[0] == '0');
+  }
   if (ce == cudaSuccess && m.family == GBN_FAMILY_LOGREG && m.precision == GBN_PREC_BF16X3) {
     if (!logreg_tc_supported(m)) {
       gbn_destroy(h);
@@ -390,24 +403,65 @@ static cudaError_t upload_params(gbn_handle h, cudaStream_t st) {
   return cudaMemcpyAsync(h->dP, &h->hp, sizeof(AdvParams), cudaMemcpyHostToDevice, st);
 }
 
-// Alternate advance/potential until no chain is active.  Returns GBN status.
+// One batch of TICK_BATCH ticks: advance + potential, parities 0, 1, 0, ... (so every batch
+// issues the same launches with the same arguments; the kernels read their parameters from
+// device memory).
+constexpr int TICK_BATCH = 16;
+static cudaError_t launch_tick_batch(gbn_handle h, cudaStream_t st) {
+  for (int k = 0; k < TICK_BATCH; ++k) {
+    const int parity = k & 1;
+    launch_advance(h->dP, h->C, h->D, h->cta_per_chain, parity, st);
+    cudaError_t e = launch_potential(h->m, h->e.Q, h->C, h->e.PE, h->e.G, h->counters + 2 * parity, st);
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
+// Capture one batch on the private capture stream (nothing executes) and instantiate it.
+// Any failure turns graphs off for this handle; the direct launches remain.
+static void capture_tick_graph(gbn_handle h) {
+  cudaGraph_t g = nullptr;
+  cudaError_t e = cudaStreamBeginCapture(h->cap_stream, cudaStreamCaptureModeThreadLocal);
+  if (e == cudaSuccess) {
+    cudaError_t el = launch_tick_batch(h, h->cap_stream);
+    e = cudaStreamEndCapture(h->cap_stream, &g);
+    if (el != cudaSuccess) e = el;
+  }
+  if (e == cudaSuccess) e = cudaGraphInstantiate(&h->tick_graph, g, 0);
+  if (g) cudaGraphDestroy(g);
+  if (e != cudaSuccess) {
+    h->tick_graph = nullptr;
+    h->use_graphs = 0;
+    cudaGetLastError();  // capture errors are not sticky; clear the last-error slot
+  } else {
+    h->graph_scratch = h->m.part_g ? (void*)h->m.part_g : (void*)h->m.resid;
+  }
+}
+
+// Alternate advance/potential until no chain is active.  Returns GBN status.  After the first
+// batch has run directly (allocating any scratch on the way), later batches replay one CUDA
+// graph of the batch.
 static int tick_loop(gbn_handle h, cudaStream_t st, int64_t max_ticks) {
-  int parity = 0;
   int64_t ticks = 0;
-  const int batch = 16;
   int64_t launches = 0;
   for (;;) {
-    int last = 0;
-    for (int k = 0; k < batch; ++k) {
-      launch_advance(h->dP, h->C, h->D, h->cta_per_chain, parity, st);
-      cudaError_t e = launch_potential(h->m, h->e.Q, h->C, h->e.PE, h->e.G, h->counters + 2 * parity, st);
-      if (e != cudaSuccess) return cuda_fail(h, e, "tick launch");
-      last = parity;
-      parity ^= 1;
-      ++ticks;
-      ++launches;
+    const int last = (TICK_BATCH - 1) & 1;
+    void* scratch = h->m.part_g ? (void*)h->m.part_g : (void*)h->m.resid;
+    if (h->tick_graph && h->graph_scratch != scratch) {  // scratch was reallocated since the capture
+      cudaGraphExecDestroy(h->tick_graph);
+      h->tick_graph = nullptr;
     }
-    cudaError_t e = cudaMemcpyAsync(h->h_counters, h->counters, sizeof(int32_t) * 4, cudaMemcpyDeviceToHost, st);
+    cudaError_t e;
+    if (h->tick_graph) {
+      e = cudaGraphLaunch(h->tick_graph, st);
+    } else {
+      e = launch_tick_batch(h, st);
+      if (e == cudaSuccess && h->use_graphs && ticks > 0) capture_tick_graph(h);
+    }
+    if (e != cudaSuccess) return cuda_fail(h, e, "tick launch");
+    ticks += TICK_BATCH;
+    launches += TICK_BATCH;
+    e = cudaMemcpyAsync(h->h_counters, h->counters, sizeof(int32_t) * 4, cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return cuda_fail(h, e, "tick loop");
     if (h->m.tc && logreg_tc_error(h->m))

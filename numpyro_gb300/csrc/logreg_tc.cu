@@ -190,6 +190,8 @@ __device__ __forceinline__ float tanh_approx(float x) {
 // One tile of the epilogue for one warp: its lane's chain x 32 rows (TMEM columns at taddr).
 // TMEM holds h = l'/2 (the coefficients enter GEMM1 halved, an exact scaling).  Per row:
 //   E = sigmoid(l') = tanh(h)/2 + 1/2                      -> bf16, K-major tile for GEMM2
+//       (forming it by Newton's method on the FMA pipe for half the rows measured slower:
+//       with 2.125 special-function ops per logit the epilogue is issue-bound)
 //   softplus(l') - l'/2 = |h| + log(1 + e^{-2|h|})          -> |h| summed, the logs taken as
 //                                                            one log2 per product of 8 rows
 // With MASK, rows r >= nvalid lie past the end of the data: they are left out of the
@@ -224,7 +226,7 @@ __device__ __forceinline__ void epilogue_tile(uint32_t taddr, uint8_t* erow, int
         const float t = ex2_approx(fabsf(h) * NEG_2LOG2E);  // e^{-|l'|}
         if (!MASK || r < nvalid) {
           ta += fabsf(h);
-          prod *= 1.0f + t;
+          prod = fmaf(prod, t, prod);  // prod * (1 + t), one rounding
         }
         ev[hh] = fmaf(0.5f, tanh_approx(h), 0.5f);
       }

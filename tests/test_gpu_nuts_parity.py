@@ -192,3 +192,27 @@ def test_uneven_batched_models_match_single_model_runs():
     D2 = m2.latent_dim
     np.testing.assert_array_equal(outb[4:6, :, :D2], out2[4:6])
     assert np.all(outb[4:6, :, D2:] == 0)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("family", ["hier", "logreg"])
+def test_tick_graph_replay_matches_direct_launches(family, monkeypatch):
+    """Batches of ticks replayed from a captured CUDA graph give the draws of launching every
+    kernel directly (GBN_CUDA_GRAPHS=0), bit for bit."""
+    if family == "hier":
+        model, _ = _hier()
+        C, kw = 16, dict(engine="ticks")
+    else:
+        X, yv, _ = datasets.covtype_like(seed=5, n=4000, n_cont=3, n_bin=4)
+        model = models.LogisticRegression(X, yv)
+        C, kw = 64, dict(engine="fused", precision="fp32")
+    res = []
+    for graphs in ("1", "0"):
+        monkeypatch.setenv("GBN_CUDA_GRAPHS", graphs)
+        k = NUTS(model, num_chains=C, **kw)
+        st = k.init(SEED, 40)
+        out = k.run_device(st, 80, collect_start=0, collect=("z", "num_steps"))
+        res.append((out["z"].cpu().numpy(), out["num_steps"].cpu().numpy()))
+        k.close()
+    np.testing.assert_array_equal(res[0][0], res[1][0])
+    np.testing.assert_array_equal(res[0][1], res[1][1])
