@@ -97,7 +97,7 @@ typedef struct {
   int32_t max_tree_depth;
   int32_t adapt_step_size;
   int32_t adapt_mass_matrix;
-  int32_t dense_mass; /* only 0 is supported by this build */
+  int32_t dense_mass; /* 1: full mass matrices ([C][D][D] in gbn_state), latent dim <= 1024, not SV */
   int32_t regularize_mass_matrix;
   int32_t find_heuristic_step_size;
   int32_t num_steps; /* HMC: fixed number of steps, 0 = from trajectory_length */
@@ -109,7 +109,10 @@ typedef struct {
 } gbn_config;
 
 /* HMCState (numpyro/infer/hmc.py:31-47) + HMCAdaptState (hmc_util.py:18-30)
- * as caller-owned device buffers, chain-major.  C = num_chains, D = latent dim. */
+ * as caller-owned device buffers, chain-major.  C = num_chains, D = latent dim.
+ * With dense_mass the three mass matrices are [C][D][D] row-major (inverse_mass_matrix
+ * symmetric, mass_matrix_sqrt and mass_matrix_sqrt_inv lower triangular) and mm_m2 is
+ * [C][D][D]; gbn_init's d_inverse_mass_matrix is then [C][D][D] as well. */
 typedef struct {
   int32_t* i;                   /* [C] iteration */
   float* z;                     /* [C][D] unconstrained position */
@@ -121,12 +124,12 @@ typedef struct {
   float* mean_accept_prob;      /* [C] */
   uint8_t* diverging;           /* [C] */
   float* step_size;             /* [C] adapt_state.step_size */
-  float* inverse_mass_matrix;   /* [C][D] diagonal */
-  float* mass_matrix_sqrt;      /* [C][D] */
-  float* mass_matrix_sqrt_inv;  /* [C][D] */
+  float* inverse_mass_matrix;   /* [C][D] diagonal ([C][D][D] dense) */
+  float* mass_matrix_sqrt;      /* [C][D] ([C][D][D] dense) */
+  float* mass_matrix_sqrt_inv;  /* [C][D] ([C][D][D] dense) */
   double* ss_state;             /* [C][5] dual averaging (x_t, x_avg, g_avg, t, prox_center) */
   double* mm_mean;              /* [C][D] Welford mean */
-  double* mm_m2;                /* [C][D] Welford m2 */
+  double* mm_m2;                /* [C][D] Welford m2 ([C][D][D] dense) */
   int32_t* mm_n;                /* [C] */
   int32_t* window_idx;          /* [C] */
   uint32_t* rng_key;            /* [C][2] (chain id, transition counter) */

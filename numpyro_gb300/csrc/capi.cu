@@ -173,7 +173,6 @@ int gbn_create(gbn_handle* out, const gbn_model_desc* md, const gbn_config* cfg)
   if (!out || !md || !cfg) return fail(nullptr, GBN_ERR_INVALID_ARG, "gbn_create: null argument");
   *out = nullptr;
   if (cfg->num_chains <= 0) return fail(nullptr, GBN_ERR_INVALID_ARG, "num_chains must be positive");
-  if (cfg->dense_mass) return fail(nullptr, GBN_ERR_UNSUPPORTED, "dense_mass=True is not supported by this engine");
   if (cfg->algo != GBN_ALGO_NUTS && cfg->algo != GBN_ALGO_HMC)
     return fail(nullptr, GBN_ERR_INVALID_ARG, "algo must be NUTS or HMC");
   if (cfg->max_tree_depth < 1 || cfg->max_tree_depth > 20 || cfg->max_tree_depth_warmup < 1 ||
@@ -295,6 +294,13 @@ int gbn_create(gbn_handle* out, const gbn_model_desc* md, const gbn_config* cfg)
                     &e.g_p, &e.z_sp, &e.g_sp, &e.rsum, &e.rsum_sub, &e.Q, &e.G};
   for (float** v : vecs)
     if (ce == cudaSuccess) ce = dalloc(h, v, CD);
+  if (cfg->dense_mass && (m.family == GBN_FAMILY_SV || D > 1024)) {
+    gbn_destroy(h);
+    return fail(nullptr, GBN_ERR_UNSUPPORTED,
+                "dense_mass=True needs a latent dimension <= 1024 (a warp per chain; not the SV family)");
+  }
+  if (ce == cudaSuccess && cfg->dense_mass) ce = dalloc(h, &e.tmp, CD);
+  if (ce == cudaSuccess && cfg->dense_mass) ce = dalloc(h, &e.tmpd, 2 * CD);
   if (ce == cudaSuccess) ce = dalloc(h, &e.r_ck, CD * h->maxd);
   if (ce == cudaSuccess) ce = dalloc(h, &e.rs_ck, CD * h->maxd);
   if (ce == cudaSuccess) ce = dalloc(h, &e.PE, (size_t)C);
@@ -362,6 +368,7 @@ int gbn_create(gbn_handle* out, const gbn_model_desc* md, const gbn_config* cfg)
   P.regularize = cfg->regularize_mass_matrix;
   P.heuristic = cfg->find_heuristic_step_size;
   P.lockstep = (cfg->engine == GBN_ENGINE_PLAIN);
+  P.dense = cfg->dense_mass ? 1 : 0;
   P.fixed_steps = cfg->num_steps;
   P.target_accept = (float)cfg->target_accept_prob;
   P.max_dE = cfg->max_delta_energy > 0 ? cfg->max_delta_energy : 1000.0;
@@ -410,7 +417,7 @@ constexpr int TICK_BATCH = 16;
 static cudaError_t launch_tick_batch(gbn_handle h, cudaStream_t st) {
   for (int k = 0; k < TICK_BATCH; ++k) {
     const int parity = k & 1;
-    launch_advance(h->dP, h->C, h->D, h->cta_per_chain, parity, st);
+    launch_advance(h->dP, h->C, h->D, h->cta_per_chain, h->hp.dense != 0, parity, st);
     cudaError_t e = launch_potential(h->m, h->e.Q, h->C, h->e.PE, h->e.G, h->counters + 2 * parity, st);
     if (e != cudaSuccess) return e;
   }
@@ -531,7 +538,8 @@ int gbn_init(gbn_handle h, void* stream, int32_t num_warmup, const float* d_init
       return fail(h, GBN_ERR_INIT_FAILED,
                   "Cannot find valid initial parameters. Please check your model again.");
   }
-  launch_init_state(h->dP, C, D, d_inv_mass, (float)h->cfg.init_step_size, s);
+  launch_init_state(h->dP, C, D, h->hp.dense ? nullptr : d_inv_mass, (float)h->cfg.init_step_size, s);
+  if (h->hp.dense) launch_init_dense_mass(h->dP, C, d_inv_mass, s);
   e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_fail(h, e, "gbn_init: state");
   if (h->cfg.adapt_step_size && h->cfg.find_heuristic_step_size && num_warmup > 0) {
@@ -601,7 +609,7 @@ int gbn_run(gbn_handle h, void* stream, gbn_state* st, int32_t num_iterations, i
     } else {
       HierView hv{h->m.y, h->m.sigma, h->m.offsets, h->m.chains_per_model, h->m.num_models, h->m.hyper[0],
                   h->m.hyper[1]};
-      launch_persistent_hier(h->dP, hv, h->counters + 7, h->order, h->C, s);
+      launch_persistent_hier(h->dP, hv, h->counters + 7, h->order, h->C, h->hp.dense != 0, s);
     }
     e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);

@@ -199,9 +199,11 @@ struct EngineBufs {
   double* PE;    // potentials returned by the potential
   ChainCtl* ctl;
   int32_t* chain_dim;  // [C] per-chain latent dim (uneven models) or nullptr
+  float* tmp;          // dense mass matrix: [C][D] vector scratch (nullptr otherwise)
+  double* tmpd;        // dense mass matrix: [C][2][D] Welford deltas (nullptr otherwise)
 };
 
-struct StateBufs {  // mirrors gbn_state
+struct StateBufs {  // mirrors gbn_state (mass matrices and mm_m2 are [C][D][D] when dense)
   int32_t* i;
   float* z;
   float* z_grad;
@@ -246,6 +248,7 @@ struct AdvParams {
   int32_t algo;
   int32_t adapt_step, adapt_mass, regularize, heuristic;
   int32_t lockstep;
+  int32_t dense;  // mass matrices [C][D][D] (dense_mass=True) instead of [C][D]
   int32_t fixed_steps;
   int32_t collect_start, thinning, num_collect;
   float target_accept;

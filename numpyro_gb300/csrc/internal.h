@@ -58,14 +58,15 @@ inline int pad4(int v) { return (v + 3) & ~3; }
 
 // nuts_engine.cu
 // a CTA per chain when cta_per_chain or D > 1024, else a warp per chain
-void launch_advance(const AdvParams* dP, int C, int D, bool cta_per_chain, int parity, cudaStream_t st);
+void launch_advance(const AdvParams* dP, int C, int D, bool cta_per_chain, bool dense, int parity, cudaStream_t st);
 void launch_persistent_hier(const AdvParams* dP, const HierView& hv, int32_t* queue_head, const int32_t* order,
-                            int C, cudaStream_t st);
+                            int C, bool dense, cudaStream_t st);
 void launch_persistent_sv(const AdvParams* dP, const SvView& sv, int32_t* queue_head, int C, cudaStream_t st);
 void launch_init_uniform(const AdvParams* dP, int C, int D, int attempt, const int32_t* flag, cudaStream_t st);
 void launch_check_valid(const AdvParams* dP, int C, int32_t* flag, int32_t* count, cudaStream_t st);
 void launch_init_state(const AdvParams* dP, int C, int D, const float* inv_mass_init, float init_step,
                        cudaStream_t st);
+void launch_init_dense_mass(const AdvParams* dP, int C, const float* inv_mass_init, cudaStream_t st);
 void launch_set_phase(const AdvParams* dP, int C, int phase, int iters, cudaStream_t st);
 void launch_set_rng_chain(uint32_t* rng_key, int C, int first_chain, cudaStream_t st);
 

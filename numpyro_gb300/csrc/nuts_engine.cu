@@ -34,7 +34,55 @@ namespace gbn {
 constexpr float FLT32_TINY = 1.17549435e-38f;
 constexpr float FLT32_MAX = 3.40282347e+38f;
 
+// ------------------------------------------------------------------ dense mass matrix
+// From a symmetric positive-definite covariance A (FP64, row-major [ld][ld], both triangles),
+// writes the three HMCAdaptState matrices the way welford_covariance.final_fn and
+// _initialize_mass_matrix do (numpyro/infer/hmc_util.py:199-239, :439-515):
+//   inverse_mass_matrix  = A
+//   mass_matrix_sqrt_inv = T, lower triangular with A = T^T T (the Cholesky factor of A with its
+//                          index order reversed: A = U U^T, U upper, T = U^T)
+//   mass_matrix_sqrt     = S = T^-1 (lower), so M = A^-1 = S S^T and momentum r = S eps.
+// The factorisation runs in FP64 in place (U in the upper triangle, S below the diagonal); A is
+// zeroed afterwards (it is the Welford m2 buffer, reset at every window end).  One group per
+// matrix; threads own columns.
 template <int NT>
+__device__ void dense_factor(const Group<NT>& g, double* A, int D, int ld, float* inv, float* sq, float* sqi) {
+  for (int j = g.tid; j < D; j += NT)
+    for (int i = 0; i < D; ++i) inv[(size_t)i * ld + j] = (float)A[(size_t)i * ld + j];
+  for (int k = D - 1; k >= 0; --k) {
+    g.sync();
+    const double ukk = sqrt(A[(size_t)k * ld + k]);
+    for (int i = g.tid; i < k; i += NT) A[(size_t)i * ld + k] /= ukk;  // U[i][k]
+    g.sync();
+    if (g.tid == 0) A[(size_t)k * ld + k] = ukk;
+    // trailing update of the leading k x k block (upper triangle): A[i][j] -= U[i][k] U[j][k]
+    for (int j = g.tid; j < k; j += NT) {
+      const double ujk = A[(size_t)j * ld + k];
+      for (int i = 0; i <= j; ++i) A[(size_t)i * ld + j] -= A[(size_t)i * ld + k] * ujk;
+    }
+  }
+  g.sync();
+  // S = T^-1 column by column (T[r][m] = U[m][r] = A[m][r] for m <= r); S[r][c] -> A[r][c], r > c
+  for (int cc = g.tid; cc < D; cc += NT) {
+    const double scc = 1.0 / A[(size_t)cc * ld + cc];
+    for (int r = cc + 1; r < D; ++r) {
+      double acc = A[(size_t)cc * ld + r] * scc;  // m = cc
+      for (int m = cc + 1; m < r; ++m) acc += A[(size_t)m * ld + r] * A[(size_t)m * ld + cc];
+      A[(size_t)r * ld + cc] = -acc / A[(size_t)r * ld + r];
+    }
+    for (int r = 0; r < D; ++r) {
+      const size_t o = (size_t)r * ld + cc;
+      sqi[o] = (r >= cc) ? (float)A[(size_t)cc * ld + r] : 0.0f;
+      sq[o] = (r > cc) ? (float)A[o] : (r == cc ? (float)scc : 0.0f);
+    }
+  }
+  g.sync();
+  for (int j = g.tid; j < D; j += NT)
+    for (int i = 0; i < D; ++i) A[(size_t)i * ld + j] = 0.0;
+  g.sync();
+}
+
+template <int NT, bool DM = false>  // DM: dense mass matrices
 struct Chain {
   const AdvParams& P;
   Group<NT> g;
@@ -81,6 +129,7 @@ struct Chain {
   // the subtree sum rs - rs_minus + rs_plus of _is_iterative_turning when rs_minus is given
   __device__ bool is_turning(const float* rl, const float* rr, const float* rs, const float* rs_minus,
                              const float* rs_plus) {
+    if (DM) return is_turning_dense(rl, rr, rs, rs_minus, rs_plus);
     const float* mi = V(P.s.inverse_mass_matrix);
     float ax = 0.0f, ay = 0.0f;
     for (int d0 = g.tid; d0 < D; d0 += UB * NT) {
@@ -119,6 +168,64 @@ struct Chain {
     }
   }
 
+  // ----------------------------------------------------------- dense mass matrix helpers
+  // [D][D] matrices of this chain (row stride ld)
+  __device__ __forceinline__ float* MX(float* base) const { return base + (size_t)c * ld * ld; }
+  // use(d, (A x)_d) for this thread's elements d, A symmetric (read by columns: A[j][d]); x is
+  // read in full, so the group must have synchronised after writing it
+  template <typename F>
+  __device__ void sym_matvec(const float* A, const float* x, F&& use) {
+    for (int d0 = g.tid; d0 < D; d0 += UB * NT) {
+      float acc[UB] = {0.0f, 0.0f, 0.0f, 0.0f};
+      for (int j = 0; j < D; ++j) {
+        const float xj = x[j];
+        const float* Aj = A + (size_t)j * ld + d0;
+#pragma unroll
+        for (int k = 0; k < UB; ++k)
+          if (d0 + k * NT < D) acc[k] = fmaf(Aj[k * NT], xj, acc[k]);
+      }
+#pragma unroll
+      for (int k = 0; k < UB; ++k)
+        if (d0 + k * NT < D) use(d0 + k * NT, acc[k]);
+    }
+  }
+  // 0.5 r . (M^-1 r) with a dense M^-1 (euclidean_kinetic_energy, hmc_util.py:1183-1200)
+  __device__ double kinetic_dense(const float* r) {
+    g.sync();
+    float acc = 0.0f;
+    sym_matvec(MX(P.s.inverse_mass_matrix), r, [&](int d, float v) { acc = fmaf(v, r[d], acc); });
+    return 0.5 * ff_value(g.sumff(ff_from(acc), red));
+  }
+  // _is_turning with a dense M^-1: v_l . s = r_l . (M^-1 s) as M^-1 is symmetric
+  __device__ bool is_turning_dense(const float* rl, const float* rr, const float* rs, const float* rs_minus,
+                                   const float* rs_plus) {
+    float* sv = V(P.e.tmp);
+    for (int d = g.tid; d < D; d += NT) {
+      float s_ = rs[d];
+      if (rs_minus) s_ = (s_ - rs_minus[d]) + rs_plus[d];
+      sv[d] = s_ - 0.5f * (rl[d] + rr[d]);
+    }
+    g.sync();
+    float ax = 0.0f, ay = 0.0f;
+    sym_matvec(MX(P.s.inverse_mass_matrix), sv, [&](int d, float w) {
+      ax = fmaf(rl[d], w, ax);
+      ay = fmaf(rr[d], w, ay);
+    });
+    FF tx = ff_from(ax), ty = ff_from(ay);
+    g.sum2ff(tx, ty, red);  // also keeps every thread's reads of sv before the next write
+    return (ff_value(tx) <= 0.0) || (ff_value(ty) <= 0.0);
+  }
+  // r = S eps (momentum_generator, hmc.py:92-110) with eps in the scratch row; S row-major
+  __device__ void dense_momentum(const float* Smat, float* r_out) {
+    const float* eps = V(P.e.tmp);
+    for (int i = g.tid; i < D; i += NT) {
+      const float* Si = Smat + (size_t)i * ld;
+      float acc = 0.0f;
+      for (int j = 0; j < D; ++j) acc = fmaf(Si[j], eps[j], acc);
+      r_out[i] = acc;
+    }
+  }
+
   // ----------------------------------------------------------- leapfrog halves
   // first half-kick + drift from the frontier on side `right`; writes Q
   __device__ void leaf_prepare(bool right, float eps) {
@@ -127,6 +234,16 @@ struct Chain {
     const float* gr = V(right ? P.e.g_r : P.e.g_l);
     const float* mi = V(P.s.inverse_mass_matrix);
     float* q = V(P.e.Q);
+    if (DM) {  // r_half = r - eps/2 g; z += eps M^-1 r_half
+      for (int d = g.tid; d < D; d += NT) r[d] = r[d] - 0.5f * eps * gr[d];
+      g.sync();
+      sym_matvec(MX(P.s.inverse_mass_matrix), r, [&](int d, float v) {
+        const float zn = z[d] + eps * v;
+        z[d] = zn;
+        q[d] = zn;
+      });
+      return;
+    }
     for (int d0 = g.tid; d0 < D; d0 += UB * NT) {
       float zz[UB], rr[UB], gg[UB], mm[UB];
 #pragma unroll
@@ -156,6 +273,14 @@ struct Chain {
     float* gr = V(right ? P.e.g_r : P.e.g_l);
     const float* G = V(P.e.G);
     const float* mi = V(P.s.inverse_mass_matrix);
+    if (DM) {
+      for (int d = g.tid; d < D; d += NT) {
+        const float gn = G[d];
+        r[d] = r[d] - 0.5f * eps * gn;
+        gr[d] = gn;
+      }
+      return kinetic_dense(r);
+    }
     float acc = 0.0f;  // kinetic energy of the new momentum, as kinetic()
     for (int d0 = g.tid; d0 < D; d0 += UB * NT) {
       float gn[UB], rr[UB], mm[UB];
@@ -194,7 +319,23 @@ struct Chain {
     float *gl = V(P.e.g_l), *grr = V(P.e.g_r), *gp = V(P.e.g_p);
     float kin = 0.0f;
     const float* mi = V(P.s.inverse_mass_matrix);
-    for (int d0 = g.tid; d0 < D; d0 += UB * NT) {
+    double kin_dense = 0.0;
+    if (DM) {  // eps -> scratch; r = S eps; K = r . (M^-1 r) / 2
+      float* eps = V(P.e.tmp);
+      for (int d = g.tid; d < D; d += NT) {
+        eps[d] = normal_at(P.seed, chain_id, n, P_MOMENTUM, d, 0);
+        zl[d] = z[d]; zr[d] = z[d]; zp[d] = z[d];
+        gl[d] = gz[d]; grr[d] = gz[d]; gp[d] = gz[d];
+      }
+      g.sync();
+      dense_momentum(MX(P.s.mass_matrix_sqrt), rl);
+      for (int d = g.tid; d < D; d += NT) {
+        rr[d] = rl[d];
+        rs[d] = rl[d];
+      }
+      kin_dense = kinetic_dense(rl);
+    }
+    for (int d0 = g.tid; d0 < D && !DM; d0 += UB * NT) {
       float msv[UB], miv[UB], zv[UB], gv[UB];
 #pragma unroll
       for (int k = 0; k < UB; ++k) {
@@ -216,7 +357,7 @@ struct Chain {
         rl[d] = r; rr[d] = r; rs[d] = r;
       }
     }
-    const double kin0 = 0.5 * ff_value(g.sumff(ff_from(kin), red));
+    const double kin0 = DM ? kin_dense : 0.5 * ff_value(g.sumff(ff_from(kin), red));
     int i = P.s.i[c];
     double pe = P.s.potential_energy[c];
     ctl.energy0 = pe + kin0;
@@ -430,16 +571,34 @@ struct Chain {
     bool middle = (0 < widx) && (widx < P.num_windows - 1);
     const float* z = V(P.s.z);
     double* mean = P.s.mm_mean + row();
-    double* m2 = P.s.mm_m2 + row();
+    double* m2 = DM ? P.s.mm_m2 + (size_t)c * ld * ld : P.s.mm_m2 + row();
     if (P.adapt_mass && middle) {  // welford update_fn
       nn += 1;
       const double inv_n = 1.0 / (double)nn;
-      for (int d = g.tid; d < D; d += NT) {
-        double x = (double)z[d];
-        double dpre = x - mean[d];
-        double mnew = mean[d] + dpre * inv_n;
-        mean[d] = mnew;
-        m2[d] += dpre * (x - mnew);
+      if (DM) {  // m2 += outer(delta_post, delta_pre)
+        double* dpost = P.e.tmpd + (size_t)c * 2 * ld;
+        double* dpre = dpost + ld;
+        for (int d = g.tid; d < D; d += NT) {
+          const double x = (double)z[d];
+          const double dp = x - mean[d];
+          const double mnew = mean[d] + dp * inv_n;
+          mean[d] = mnew;
+          dpre[d] = dp;
+          dpost[d] = x - mnew;
+        }
+        g.sync();
+        for (int j = g.tid; j < D; j += NT) {
+          const double pj = dpre[j];
+          for (int i = 0; i < D; ++i) m2[(size_t)i * ld + j] += dpost[i] * pj;
+        }
+      } else {
+        for (int d = g.tid; d < D; d += NT) {
+          double x = (double)z[d];
+          double dpre = x - mean[d];
+          double mnew = mean[d] + dpre * inv_n;
+          mean[d] = mnew;
+          m2[d] += dpre * (x - mnew);
+        }
       }
       if (g.tid == 0) P.s.mm_n[c] = nn;
     }
@@ -448,7 +607,21 @@ struct Chain {
     if (g.tid == 0) P.s.window_idx[c] = widx;
     bool started = false;
     if (at_end && middle) {
-      if (P.adapt_mass) {  // welford final_fn + Stan regularisation (nn counts this draw)
+      if (DM && P.adapt_mass) {  // welford final_fn (dense) + Stan regularisation
+        const double a = P.regularize ? (double)nn / (nn + 5.0) : 1.0;
+        const double shrink = P.regularize ? 1e-3 * (5.0 / (nn + 5.0)) : 0.0;
+        const double inv_nm1 = 1.0 / (double)(nn - 1);
+        g.sync();
+        for (int j = g.tid; j < D; j += NT)
+          for (int i = 0; i < D; ++i) {
+            const size_t o = (size_t)i * ld + j;
+            m2[o] = a * (m2[o] * inv_nm1) + (i == j ? shrink : 0.0);
+          }
+        dense_factor(g, m2, D, ld, MX(P.s.inverse_mass_matrix), MX(P.s.mass_matrix_sqrt),
+                     MX(P.s.mass_matrix_sqrt_inv));
+        for (int d = g.tid; d < D; d += NT) mean[d] = 0.0;
+        if (g.tid == 0) P.s.mm_n[c] = 0;
+      } else if (P.adapt_mass) {  // welford final_fn + Stan regularisation (nn counts this draw)
         float* inv = V(P.s.inverse_mass_matrix);
         float* sq = V(P.s.mass_matrix_sqrt);
         float* sqi = V(P.s.mass_matrix_sqrt_inv);
@@ -504,6 +677,23 @@ struct Chain {
     float* r0 = V(P.e.r_l);
     float* rh = V(P.e.r_r);
     float* q = V(P.e.Q);
+    if (DM) {
+      // the trial momentum is M^-1 eps, as momentum_generator(z, inverse_mass_matrix, key) at
+      // hmc_util.py:356 (the dense inverse mass matrix stands in for the square root there)
+      float* epsv = V(P.e.tmp);
+      for (int d = g.tid; d < D; d += NT)
+        epsv[d] = normal_at(P.seed, chain_id, (uint32_t)ctl.hmc_total, P_HEURISTIC, d, (uint32_t)ctl.heur_trial);
+      g.sync();
+      sym_matvec(MX(P.s.inverse_mass_matrix), epsv, [&](int d, float v) {
+        r0[d] = v;
+        rh[d] = v - 0.5f * eps * gz[d];
+      });
+      const double k0 = kinetic_dense(r0);  // synchronises after r0 and rh were written
+      sym_matvec(MX(P.s.inverse_mass_matrix), rh, [&](int d, float v) { q[d] = z[d] + eps * v; });
+      ctl.heur_e0 = P.s.potential_energy[c] + k0;
+      ctl.phase = PH_HEUR;
+      return;
+    }
     float kin = 0.0f;
     for (int d = g.tid; d < D; d += NT) {
       float r = mi[d] * normal_at(P.seed, chain_id, (uint32_t)ctl.hmc_total, P_HEURISTIC, d,
@@ -523,12 +713,19 @@ struct Chain {
     const float* mi = V(P.s.inverse_mass_matrix);
     const float* G = V(P.e.G);
     const float* rh = V(P.e.r_r);
-    float kin = 0.0f;
-    for (int d = g.tid; d < D; d += NT) {
-      float rn = rh[d] - 0.5f * eps * G[d];
-      kin = fmaf(mi[d] * rn, rn, kin);
+    double e_new;
+    if (DM) {
+      float* rn = V(P.e.r_r);  // r_new overwrites r_half in place
+      for (int d = g.tid; d < D; d += NT) rn[d] = rn[d] - 0.5f * eps * G[d];
+      e_new = P.e.PE[c] + kinetic_dense(rn);
+    } else {
+      float kin = 0.0f;
+      for (int d = g.tid; d < D; d += NT) {
+        float rn = rh[d] - 0.5f * eps * G[d];
+        kin = fmaf(mi[d] * rn, rn, kin);
+      }
+      e_new = P.e.PE[c] + 0.5 * ff_value(g.sumff(ff_from(kin), red));
     }
-    double e_new = P.e.PE[c] + 0.5 * ff_value(g.sumff(ff_from(kin), red));
     double dE = e_new - ctl.heur_e0;
     int dir_new = (log(0.8) < -dE) ? 1 : -1;
     ctl.heur_last = ctl.heur_dir;
@@ -714,7 +911,7 @@ struct Chain {
   }
 };
 
-template <int NT>
+template <int NT, bool DM>
 __global__ void __launch_bounds__(256) advance_kernel(const AdvParams* __restrict__ Pp, int parity) {
   __shared__ double red[16];
   const AdvParams& P = *Pp;
@@ -733,7 +930,7 @@ __global__ void __launch_bounds__(256) advance_kernel(const AdvParams* __restric
   }
   int pending = 0, active = 0;
   if (c < P.C) {
-    Chain<NT> ch{P, Group<NT>{tid}, red, c, P.e.chain_dim ? P.e.chain_dim[c] : P.D, P.D, P.e.ctl[c]};
+    Chain<NT, DM> ch{P, Group<NT>{tid}, red, c, P.e.chain_dim ? P.e.chain_dim[c] : P.D, P.D, P.e.ctl[c]};
     ch.run();
     if (tid == 0) {
       P.e.ctl[c] = ch.ctl;
@@ -790,13 +987,15 @@ __global__ void init_state_kernel(const AdvParams* __restrict__ Pp, const float*
   for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < total; k += (size_t)gridDim.x * blockDim.x) {
     int c = (int)(k / P.D), d = (int)(k % P.D);
     int Dc = P.e.chain_dim ? P.e.chain_dim[c] : P.D;
-    float inv = (d < Dc) ? (inv_mass_init ? inv_mass_init[k] : 1.0f) : 0.0f;
-    float si = sqrtf(inv);
-    P.s.inverse_mass_matrix[k] = inv;
-    P.s.mass_matrix_sqrt_inv[k] = si;
-    P.s.mass_matrix_sqrt[k] = (d < Dc) ? 1.0f / si : 0.0f;
+    if (!P.dense) {  // dense mass matrices are set by init_dense_mass_kernel
+      float inv = (d < Dc) ? (inv_mass_init ? inv_mass_init[k] : 1.0f) : 0.0f;
+      float si = sqrtf(inv);
+      P.s.inverse_mass_matrix[k] = inv;
+      P.s.mass_matrix_sqrt_inv[k] = si;
+      P.s.mass_matrix_sqrt[k] = (d < Dc) ? 1.0f / si : 0.0f;
+      P.s.mm_m2[k] = 0.0;
+    }
     P.s.mm_mean[k] = 0.0;
-    P.s.mm_m2[k] = 0.0;
     if (d == 0) {
       P.s.i[c] = 0;
       P.s.num_steps[c] = 0;
@@ -813,6 +1012,31 @@ __global__ void init_state_kernel(const AdvParams* __restrict__ Pp, const float*
       P.s.energy[c] = P.s.potential_energy[c];
     }
   }
+}
+
+// Dense mass matrices at init (_initialize_mass_matrix, hmc_util.py:439-515): the identity, or
+// the factorisation of a given [C][D][D] inverse mass matrix; zeroes the Welford m2.  A warp per
+// chain.
+__global__ void init_dense_mass_kernel(const AdvParams* __restrict__ Pp, const float* __restrict__ inv_mass_init) {
+  const AdvParams& P = *Pp;
+  const int c = blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (c >= P.C) return;
+  const int ld = P.D, Dc = P.e.chain_dim ? P.e.chain_dim[c] : P.D;
+  const size_t base = (size_t)c * ld * ld;
+  double* A = P.s.mm_m2 + base;
+  float *inv = P.s.inverse_mass_matrix + base, *sq = P.s.mass_matrix_sqrt + base,
+        *sqi = P.s.mass_matrix_sqrt_inv + base;
+  for (size_t o = lane; o < (size_t)ld * ld; o += 32) {
+    const int i = (int)(o / ld), j = (int)(o % ld);
+    const float id = (i == j && i < Dc) ? 1.0f : 0.0f;
+    inv[o] = id;
+    sq[o] = id;
+    sqi[o] = id;
+    A[o] = (inv_mass_init && i < Dc && j < Dc) ? (double)inv_mass_init[base + o] : 0.0;
+  }
+  __syncwarp();
+  if (inv_mass_init) dense_factor(Group<32>{lane}, A, Dc, ld, inv, sq, sqi);
 }
 
 __global__ void set_phase_kernel(const AdvParams* __restrict__ Pp, int phase, int iters) {
@@ -840,6 +1064,7 @@ __global__ void set_rng_chain_kernel(uint32_t* rng_key, int C, int first_chain) 
 // tree doubling, leaves, U-turn checks, adaptation, collection -- calling the
 // warp-level potential inline between state-machine steps.  Chains never wait for
 // one another; there is no grid-wide synchronisation and no spin-wait.
+template <bool DM>
 __global__ void __launch_bounds__(256) persistent_hier_kernel(const AdvParams* __restrict__ Pp, HierView hv,
                                                               int32_t* queue_head, const int32_t* __restrict__ order) {
   const AdvParams& P = *Pp;
@@ -853,7 +1078,7 @@ __global__ void __launch_bounds__(256) persistent_hier_kernel(const AdvParams* _
     int m = c / hv.cpm;
     if (m >= hv.num_models) m = hv.num_models - 1;
     const int j0 = hv.off[m], J = hv.off[m + 1] - j0;
-    Chain<32> ch{P, Group<32>{lane}, nullptr, c, P.e.chain_dim ? P.e.chain_dim[c] : P.D, P.D, P.e.ctl[c]};
+    Chain<32, DM> ch{P, Group<32>{lane}, nullptr, c, P.e.chain_dim ? P.e.chain_dim[c] : P.D, P.D, P.e.ctl[c]};
     ch.run();
     for (;;) {
       const int ph = ch.ctl.phase;
@@ -906,16 +1131,22 @@ __global__ void __launch_bounds__(256) persistent_sv_kernel(const AdvParams* __r
 
 // --------------------------------------------------------------------- launchers
 void launch_persistent_hier(const AdvParams* dP, const HierView& hv, int32_t* queue_head, const int32_t* order,
-                            int C, cudaStream_t st) {
+                            int C, bool dense, cudaStream_t st) {
   int dev = 0, sms = 0, per_sm = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, persistent_hier_kernel, 256, 0);
+  if (dense)
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, persistent_hier_kernel<true>, 256, 0);
+  else
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, persistent_hier_kernel<false>, 256, 0);
   if (per_sm < 1) per_sm = 1;
   int blocks = sms * per_sm;
   int need = (C + 7) / 8;  // never more warps than chains
   if (blocks > need) blocks = need;
-  persistent_hier_kernel<<<blocks, 256, 0, st>>>(dP, hv, queue_head, order);
+  if (dense)
+    persistent_hier_kernel<true><<<blocks, 256, 0, st>>>(dP, hv, queue_head, order);
+  else
+    persistent_hier_kernel<false><<<blocks, 256, 0, st>>>(dP, hv, queue_head, order);
 }
 
 void launch_persistent_sv(const AdvParams* dP, const SvView& sv, int32_t* queue_head, int C, cudaStream_t st) {
@@ -929,12 +1160,15 @@ void launch_persistent_sv(const AdvParams* dP, const SvView& sv, int32_t* queue_
   persistent_sv_kernel<<<blocks, 256, 0, st>>>(dP, sv, queue_head);
 }
 
-void launch_advance(const AdvParams* dP, int C, int D, bool cta_per_chain, int parity, cudaStream_t st) {
+void launch_advance(const AdvParams* dP, int C, int D, bool cta_per_chain, bool dense, int parity, cudaStream_t st) {
   if (!cta_per_chain && D <= 1024) {
     int cpb = 8;
-    advance_kernel<32><<<(C + cpb - 1) / cpb, 32 * cpb, 0, st>>>(dP, parity);
+    if (dense)
+      advance_kernel<32, true><<<(C + cpb - 1) / cpb, 32 * cpb, 0, st>>>(dP, parity);
+    else
+      advance_kernel<32, false><<<(C + cpb - 1) / cpb, 32 * cpb, 0, st>>>(dP, parity);
   } else {
-    advance_kernel<256><<<C, 256, 0, st>>>(dP, parity);
+    advance_kernel<256, false><<<C, 256, 0, st>>>(dP, parity);  // dense mass needs a warp per chain
   }
 }
 
@@ -955,6 +1189,10 @@ void launch_init_state(const AdvParams* dP, int C, int D, const float* inv_mass_
   int blocks = (int)((total + 255) / 256);
   if (blocks > 4096) blocks = 4096;
   init_state_kernel<<<blocks, 256, 0, st>>>(dP, inv_mass_init, init_step);
+}
+
+void launch_init_dense_mass(const AdvParams* dP, int C, const float* inv_mass_init, cudaStream_t st) {
+  init_dense_mass_kernel<<<(C + 3) / 4, 128, 0, st>>>(dP, inv_mass_init);
 }
 
 void launch_set_phase(const AdvParams* dP, int C, int phase, int iters, cudaStream_t st) {

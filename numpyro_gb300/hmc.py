@@ -87,8 +87,10 @@ class HMC(MCMCKernel):
             raise NotImplementedError("model must be a numpyro_gb300.models registry model")
         if kinetic_fn is not None:
             raise NotImplementedError("only the Euclidean kinetic energy is supported")
-        if dense_mass not in (False, [], None):
-            raise NotImplementedError("dense mass matrices are not supported by this engine")
+        if dense_mass not in (False, True, [], None):
+            # numpyro also takes a list of site-name tuples (block-structured mass matrices)
+            raise NotImplementedError("dense_mass must be True or False (block-structured mass matrices are not "
+                                      "supported by this engine)")
         if init_strategy is not init_to_uniform:
             raise NotImplementedError("only init_to_uniform(radius=2) runs on the device")
         if type(self) is HMC:
@@ -105,7 +107,7 @@ class HMC(MCMCKernel):
         self._inverse_mass_matrix = inverse_mass_matrix
         self._adapt_step_size = adapt_step_size
         self._adapt_mass_matrix = adapt_mass_matrix
-        self._dense_mass = False
+        self._dense_mass = bool(dense_mass)
         self._target_accept_prob = target_accept_prob
         self._num_steps = num_steps
         self._trajectory_length = None if trajectory_length is None else float(trajectory_length)
@@ -161,7 +163,7 @@ class HMC(MCMCKernel):
             cfg.max_tree_depth_warmup = cfg.max_tree_depth = int(mtd)
         cfg.adapt_step_size = int(bool(self._adapt_step_size))
         cfg.adapt_mass_matrix = int(bool(self._adapt_mass_matrix))
-        cfg.dense_mass = 0
+        cfg.dense_mass = int(self._dense_mass)
         cfg.regularize_mass_matrix = int(bool(self._regularize_mass_matrix))
         cfg.find_heuristic_step_size = int(bool(self._find_heuristic_step_size))
         cfg.num_steps = int(self._num_steps or 0)
@@ -213,10 +215,11 @@ class HMC(MCMCKernel):
         f32 = dict(dtype=torch.float32, device=dev)
         f64 = dict(dtype=torch.float64, device=dev)
         i32 = dict(dtype=torch.int32, device=dev)
+        mshape = (C, D, D) if self._dense_mass else (C, D)  # HMCAdaptState mass matrices, vmapped
         adapt = HMCAdaptState(
-            torch.zeros(C, **f32), torch.zeros(C, D, **f32), torch.zeros(C, D, **f32), torch.zeros(C, D, **f32),
+            torch.zeros(C, **f32), torch.zeros(mshape, **f32), torch.zeros(mshape, **f32), torch.zeros(mshape, **f32),
             torch.zeros(C, 5, **f64),
-            (torch.zeros(C, D, **f64), torch.zeros(C, D, **f64), torch.zeros(C, **i32)),
+            (torch.zeros(C, D, **f64), torch.zeros(mshape, **f64), torch.zeros(C, **i32)),
             torch.zeros(C, **i32), torch.zeros(C, 2, dtype=torch.int32, device=dev))
         traj = self._trajectory_length if self._algo == "HMC" else None
         return HMCState(
@@ -286,7 +289,15 @@ class HMC(MCMCKernel):
             z0 = torch.as_tensor(np.asarray(init_params, np.float32).reshape(C, D), device="cuda").contiguous()
         inv0 = None
         if self._inverse_mass_matrix is not None:
-            inv = np.broadcast_to(np.asarray(self._inverse_mass_matrix, np.float32), (C, D))
+            inv = np.asarray(self._inverse_mass_matrix, np.float32)
+            if self._dense_mass:
+                if inv.shape[-1:] == (D,) and (inv.ndim == 1 or inv.shape[-2:] != (D, D)):
+                    inv = np.apply_along_axis(np.diag, -1, inv)  # a diagonal given for a dense kernel
+                inv = np.broadcast_to(inv, (C, D, D))
+            else:
+                if inv.ndim >= 2 and inv.shape[-2:] == (D, D):
+                    inv = np.diagonal(inv, axis1=-2, axis2=-1)
+                inv = np.broadcast_to(inv, (C, D))
             inv0 = torch.as_tensor(np.ascontiguousarray(inv), device="cuda")
         st = self._cstate(state)
         lib = _lib.load()

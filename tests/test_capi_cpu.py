@@ -65,8 +65,9 @@ def test_kernel_constructor_contract():
         NUTS()
     with pytest.raises(NotImplementedError):
         NUTS(potential_fn=lambda z: z)
-    with pytest.raises(NotImplementedError):
-        NUTS(m, dense_mass=True)
+    assert NUTS(m, dense_mass=True)._dense_mass
+    with pytest.raises(NotImplementedError):  # block-structured dense mass
+        NUTS(m, dense_mass=[("mu", "tau")])
     with pytest.raises(ValueError):
         HMC(m, num_steps=None, trajectory_length=None)
 
