@@ -380,8 +380,14 @@ def main():
     burst, sustained, hbm, peak_kind = measured_peaks()
     flop = 4.0 * X.shape[0] * X.shape[1] * C
     achieved = flop / (pot_ms / 1e3) / 1e12
+    # DRAM bytes (read + write) of one launch of the dominant kernel at exactly this workload, from the
+    # ncu capture summarised in profiles/ (logreg_tc_kernel / logreg_simt_kernel, 1024 chains)
+    traffic = None
+    if X.shape == (581012, 55) and C == 1024:
+        traffic = 76.69e6 if precision == "bf16x3" else 135.3e6
     roofline = {"bound": "tensor", "achieved": achieved, "peak": burst, "unit": "TFLOP/s",
-                "frac": achieved / burst, "traffic": None, "peak_kind": peak_kind + " burst bf16",
+                "frac": achieved / burst, "traffic": traffic, "traffic_unit": "bytes per launch (ncu capture)",
+                "peak_kind": peak_kind + " burst bf16",
                 "kernel": "logreg potential (%s)" % precision, "algorithmic_flop_per_launch": flop,
                 "launch_ms": pot_ms}
     # ---------------- end to end through the public API with host buffers
