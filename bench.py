@@ -135,7 +135,8 @@ def run_workload(args):
             "mean_num_steps": float(ns.mean()), "divergences": int(out["diverging"].sum().item()),
             "min_bulk_ess": ess_min, "min_bulk_ess_per_s_sampling": ess_min / samp_s,
             "min_bulk_ess_per_s_total": ess_min / (warm_s + samp_s), "rhat_max": rhat_max,
-            "ess_definition": ess_note, "ticks_sampling": ticks, "us_per_tick": 1e6 * samp_s / max(1, ticks)}
+            "ess_definition": ess_note, "ticks_sampling": ticks, "us_per_tick": 1e6 * samp_s / max(1, ticks),
+            "tuning": k.tuning()}
     print(json.dumps(line))
     k.close()
     return 0

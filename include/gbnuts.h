@@ -182,6 +182,11 @@ int gbn_run(gbn_handle h, void* stream, gbn_state* st, int32_t num_iterations,
             int32_t collect_start, int32_t thinning, gbn_collect* out);
 
 int gbn_get_stats(gbn_handle h, gbn_stats* stats);
+/* Launch shapes the autotuner chose at gbn_create for this model's potential kernels ("name=value ...",
+ * empty when nothing was tuned).  The autotuner times the candidate chains-per-CTA / tile shapes
+ * once per process for each (device, model shape, chain count); GBN_AUTOTUNE=0 in the environment
+ * keeps the defaults.  No counterpart in the reference. */
+const char* gbn_tuning(gbn_handle h);
 
 /* Largest num_points accepted by gbn_logreg_potential_noalloc. */
 #define GBN_NOALLOC_MAX_POINTS 256

@@ -49,6 +49,7 @@ struct gbn_handle_s {
   cudaStream_t cap_stream = nullptr;
   cudaGraphExec_t tick_graph = nullptr;
   void* graph_scratch = nullptr;  // potential scratch the graph was captured with
+  std::string tuning;             // launch shapes chosen by the autotuner
 };
 
 static thread_local std::string g_last_error;
@@ -354,6 +355,19 @@ int gbn_create(gbn_handle* out, const gbn_model_desc* md, const gbn_config* cfg)
     gbn_destroy(h);
     return r == GBN_ERR_CUDA ? GBN_ERR_OOM : r;
   }
+  // launch shapes of the potential from the autotuner (GBN_AUTOTUNE=0 keeps the defaults)
+  {
+    const char* at = getenv("GBN_AUTOTUNE");
+    if (!(at && at[0] == '0')) {
+      ce = cudaMemset(e.Q, 0, sizeof(float) * CD);
+      if (ce == cudaSuccess) ce = autotune_potential(m, e.Q, C, e.PE, e.G, 0, &h->tuning);
+      if (ce != cudaSuccess) {
+        int r = cuda_fail(nullptr, ce, "gbn_create: autotune");
+        gbn_destroy(h);
+        return r;
+      }
+    }
+  }
   // static parameters
   AdvParams& P = h->hp;
   P.e = e;
@@ -629,6 +643,8 @@ int gbn_run(gbn_handle h, void* stream, gbn_state* st, int32_t num_iterations, i
 }
 
 int gbn_sample(gbn_handle h, void* stream, gbn_state* st) { return gbn_run(h, stream, st, 1, 0, 1, nullptr); }
+
+const char* gbn_tuning(gbn_handle h) { return h ? h->tuning.c_str() : ""; }
 
 int gbn_get_stats(gbn_handle h, gbn_stats* stats) {
   if (!h || !stats) return fail(h, GBN_ERR_INVALID_ARG, "gbn_get_stats: null argument");

@@ -1,11 +1,23 @@
 // internal.h -- host-side declarations shared by the translation units of libgbnuts.
 #pragma once
 #include <cstdint>
+#include <string>
 #include <cuda_runtime.h>
 
 namespace gbn {
 
 struct AdvParams;
+
+// Launch shapes of the potential kernels, chosen by autotune_potential (defaults before tuning).
+// hier_cpb: chains (warps) per CTA of the hierarchical kernel; hs_tm: rows per thread of the horseshoe
+// residual GEMM (tile height 16 * hs_tm); hs_splits: row ranges of the horseshoe adjoint GEMM;
+// lr_rg: row groups of the FP32 logistic kernel (0: the allocation default).
+struct TuneParams {
+  int hier_cpb = 8;
+  int hs_tm = 4;
+  int hs_splits = 4;
+  int lr_rg = 0;
+};
 
 // Device copy of a registry model plus the scratch its potential needs.
 struct ModelDev {
@@ -22,8 +34,10 @@ struct ModelDev {
   double hyper[8] = {0};
   int precision = 0;
   // scratch (sized for scratch_points potential points)
+  TuneParams tune;
   int scratch_points = 0;
-  int row_groups = 0;
+  int row_groups = 0;       // default row groups of the FP32 logistic kernel
+  int row_groups_cap = 0;   // row groups the logistic partial buffers hold
   float* part_g = nullptr;    // [row_groups][points][64]
   double* part_ll = nullptr;  // [row_groups][points]
   float* resid = nullptr;     // horseshoe [n][points]
@@ -75,6 +89,12 @@ cudaError_t ensure_potential_scratch(ModelDev& m, int points);
 void free_potential_scratch(ModelDev& m);
 cudaError_t launch_potential(ModelDev& m, const float* Q, int npts, double* PE, float* G,
                              const int32_t* pending, cudaStream_t st);
+// Times the candidate launch shapes of this model's potential at npts points (Q: any valid
+// [npts][D] positions; PE/G outputs) and stores the fastest in m.tune.  Decisions are cached per
+// process for each (device, family, shape, points), so every handle of a shape runs the same
+// arithmetic.  report receives "name=value ..." of the choice.
+cudaError_t autotune_potential(ModelDev& m, const float* Q, int npts, double* PE, float* G, cudaStream_t st,
+                               std::string* report);
 // VJP: out[k] = cot[k] * grad U(z_k)
 cudaError_t launch_scale_rows(const double* cot, float* G, int npts, int D, cudaStream_t st);
 

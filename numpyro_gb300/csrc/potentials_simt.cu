@@ -11,7 +11,14 @@
 // (transforms.py:641-644, :2115-2118).  Per-term arithmetic is FP32, sums
 // are accumulated in FP64 so potential differences stay exact to ~1e-9
 // relative even for 581k-row likelihoods.
+#include <algorithm>
 #include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
+#include <vector>
 #include "common.cuh"
 #include "hier_potential.cuh"
 #include "internal.h"
@@ -25,14 +32,14 @@ constexpr double LOG_2 = 0.6931471805599453;
 
 // ============================================================ hierarchical (non-centred)
 // z = [mu, log tau, theta_base(J)];  warp per point; model m = point / cpm
-__global__ void __launch_bounds__(256) hier_nc_kernel(const float* __restrict__ Q, int npts, int ld,
+__global__ void __launch_bounds__(512) hier_nc_kernel(const float* __restrict__ Q, int npts, int ld,
                                                       const float* __restrict__ y, const float* __restrict__ sg,
                                                       const int32_t* __restrict__ off, int cpm, int num_models,
                                                       double mu_scale,
                                                       double tau_scale, double* __restrict__ PE,
                                                       float* __restrict__ G, const int32_t* pending) {
   if (pending && *pending == 0) return;
-  int c = blockIdx.x * 8 + (threadIdx.x >> 5);
+  int c = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);  // a warp per point
   int lane = threadIdx.x & 31;
   if (c >= npts) return;
   int m = c / cpm;
@@ -207,9 +214,12 @@ __global__ void logreg_finish_kernel(const float* __restrict__ Q, int npts, int 
 // X^T and a padded X are built once per model; beta^T is packed from the chains' positions each
 // tick.  64 x 64 tiles, 16-deep K steps double-buffered through registers; 4 x 4 outputs per
 // thread.  Residual sums of squares per (row tile, chain) leave the GEMM in FP64.
-constexpr int HS_BM = 64, HS_BN = 64, HS_BK = 16;
-constexpr int HS_SPLITS = 4;  // row ranges of the adjoint GEMM (enough CTAs for 152 SMs)
+constexpr int HS_BN = 64, HS_BK = 16;
+constexpr int HS_MIN_BM = 32;     // smallest tile height offered to the tuner
+constexpr int HS_MAX_SPLITS = 8;  // most row ranges offered to the tuner for the adjoint GEMM
 
+// TM rows per thread: tiles of (16 TM) x 64 outputs, 256 threads.
+template <int TM>
 __global__ void __launch_bounds__(256) hs_sgemm_nn_kernel(const float* __restrict__ A, int lda,
                                                           const float* __restrict__ B, int ldb, int M, int N,
                                                           int K, int k_per_split, float* __restrict__ Out, int ldo,
@@ -217,37 +227,49 @@ __global__ void __launch_bounds__(256) hs_sgemm_nn_kernel(const float* __restric
                                                           double* __restrict__ part_rr, int ld_rr,
                                                           const int32_t* pending) {
   if (pending && *pending == 0) return;
-  __shared__ __align__(16) float As[2][HS_BK][HS_BM];
+  constexpr int BM = 16 * TM;
+  constexpr int AQ = BM / 4;  // float4 per K row of the A tile
+  __shared__ __align__(16) float As[2][HS_BK][BM];
   __shared__ __align__(16) float Bs[2][HS_BK][HS_BN];
   __shared__ float rr[16][HS_BN];
   const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
-  const int m0 = blockIdx.y * HS_BM, n0 = blockIdx.x * HS_BN;
+  const int m0 = blockIdx.y * BM, n0 = blockIdx.x * HS_BN;
   const int kb = blockIdx.z * k_per_split, ke = min(K, kb + k_per_split);
-  // each thread stages one float4 of A and one of B per K step: row lk, columns 4*lc..4*lc+3
+  // per K step a thread stages one float4 of B (row lk, columns lc..lc+3) and, when tid < 4 BM,
+  // one float4 of A (row ak, columns ac..ac+3)
   const int lk = tid >> 4, lc = (tid & 15) * 4;
+  const bool a_loader = tid < HS_BK * AQ;
+  const int ak = tid / AQ, ac = (tid % AQ) * 4;
   auto load = [&](int k0, float4& av, float4& bv) {
-    const int k = k0 + lk;
     const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
-    av = (k < ke && m0 + lc < M) ? *reinterpret_cast<const float4*>(A + (size_t)k * lda + m0 + lc) : zero;
-    bv = (k < ke && n0 + lc < N) ? *reinterpret_cast<const float4*>(B + (size_t)k * ldb + n0 + lc) : zero;
+    av = (a_loader && k0 + ak < ke && m0 + ac < M)
+             ? *reinterpret_cast<const float4*>(A + (size_t)(k0 + ak) * lda + m0 + ac)
+             : zero;
+    bv = (k0 + lk < ke && n0 + lc < N) ? *reinterpret_cast<const float4*>(B + (size_t)(k0 + lk) * ldb + n0 + lc)
+                                       : zero;
   };
-  float acc[4][4] = {};
+  float acc[TM][4] = {};
   float4 av, bv;
   load(kb, av, bv);
   int buf = 0;
   for (int k0 = kb; k0 < ke; k0 += HS_BK) {
-    *reinterpret_cast<float4*>(&As[buf][lk][lc]) = av;
+    if (a_loader) *reinterpret_cast<float4*>(&As[buf][ak][ac]) = av;
     *reinterpret_cast<float4*>(&Bs[buf][lk][lc]) = bv;
     __syncthreads();
     if (k0 + HS_BK < ke) load(k0 + HS_BK, av, bv);  // next step's loads overlap this step's FMAs
 #pragma unroll
     for (int kk = 0; kk < HS_BK; ++kk) {
-      const float4 a4 = *reinterpret_cast<const float4*>(&As[buf][kk][ty * 4]);
+      float aa[TM];
+#pragma unroll
+      for (int i = 0; i < TM; i += 2) {
+        const float2 a2 = *reinterpret_cast<const float2*>(&As[buf][kk][ty * TM + i]);
+        aa[i] = a2.x;
+        aa[i + 1] = a2.y;
+      }
       const float4 b4 = *reinterpret_cast<const float4*>(&Bs[buf][kk][tx * 4]);
-      const float aa[4] = {a4.x, a4.y, a4.z, a4.w};
       const float bb[4] = {b4.x, b4.y, b4.z, b4.w};
 #pragma unroll
-      for (int i = 0; i < 4; ++i)
+      for (int i = 0; i < TM; ++i)
 #pragma unroll
         for (int j = 0; j < 4; ++j) acc[i][j] = fmaf(aa[i], bb[j], acc[i][j]);
     }
@@ -256,8 +278,8 @@ __global__ void __launch_bounds__(256) hs_sgemm_nn_kernel(const float* __restric
   float* out = Out + (size_t)blockIdx.z * split_stride;
   if (yv == nullptr) {
 #pragma unroll
-    for (int i = 0; i < 4; ++i) {
-      const int m = m0 + ty * 4 + i;
+    for (int i = 0; i < TM; ++i) {
+      const int m = m0 + ty * TM + i;
       if (m >= M) continue;
       if (n0 + tx * 4 < N)
         *reinterpret_cast<float4*>(out + (size_t)m * ldo + n0 + tx * 4) =
@@ -268,8 +290,8 @@ __global__ void __launch_bounds__(256) hs_sgemm_nn_kernel(const float* __restric
   // residual epilogue: R = y - acc, and per-chain sums of R^2 over this row tile
   float sq[4] = {0.f, 0.f, 0.f, 0.f};
 #pragma unroll
-  for (int i = 0; i < 4; ++i) {
-    const int m = m0 + ty * 4 + i;
+  for (int i = 0; i < TM; ++i) {
+    const int m = m0 + ty * TM + i;
     if (m >= M) continue;
     const float y = yv[m];
     float r[4];
@@ -419,21 +441,23 @@ cudaError_t ensure_potential_scratch(ModelDev& m, int points) {
   free_potential_scratch(m);
   cudaError_t e = cudaSuccess;
   if (m.family == 2) {
-    // row groups: enough CTAs for ~4 waves over 152 SMs
+    // row groups: enough CTAs for ~4 waves over 152 SMs; buffers hold twice that for the tuner
     int cgroups = (points + LR_CT - 1) / LR_CT;
     int64_t ntiles = (m.n + LR_RT - 1) / LR_RT;
     int rg = (int)((4 * 152 + cgroups - 1) / cgroups);
     if (rg < 1) rg = 1;
     if (rg > ntiles) rg = (int)ntiles;
     m.row_groups = rg;
-    e = cudaMalloc(&m.part_g, sizeof(float) * (size_t)rg * points * 64);
-    if (e == cudaSuccess) e = cudaMalloc(&m.part_ll, sizeof(double) * (size_t)rg * points);
+    m.row_groups_cap = (int)std::min<int64_t>(2 * (int64_t)rg, ntiles);
+    if (m.tune.lr_rg > m.row_groups_cap) m.tune.lr_rg = 0;
+    e = cudaMalloc(&m.part_g, sizeof(float) * (size_t)m.row_groups_cap * points * 64);
+    if (e == cudaSuccess) e = cudaMalloc(&m.part_ll, sizeof(double) * (size_t)m.row_groups_cap * points);
   } else if (m.family == 3) {
     const int cp = pad4(points), pp = pad4(m.p);
-    const int mt = (int)((m.n + HS_BM - 1) / HS_BM);
+    const int mt = (int)((m.n + HS_MIN_BM - 1) / HS_MIN_BM);
     e = cudaMalloc(&m.resid, sizeof(float) * (size_t)m.n * cp);
     if (e == cudaSuccess) e = cudaMalloc(&m.part_rr, sizeof(double) * (size_t)mt * cp);
-    if (e == cudaSuccess) e = cudaMalloc(&m.part_gb, sizeof(float) * (size_t)HS_SPLITS * points * pp);
+    if (e == cudaSuccess) e = cudaMalloc(&m.part_gb, sizeof(float) * (size_t)HS_MAX_SPLITS * points * pp);
     if (e == cudaSuccess) e = cudaMalloc(&m.hs_bt, sizeof(float) * (size_t)pp * cp);
   }
   if (e == cudaSuccess) {
@@ -472,8 +496,12 @@ cudaError_t launch_potential(ModelDev& m, const float* Q, int npts, double* PE, 
   const int ld = m.D;
   switch (m.family) {
     case 1:
-      hier_nc_kernel<<<(npts + 7) / 8, 256, 0, st>>>(Q, npts, ld, m.y, m.sigma, m.offsets, m.chains_per_model,
-                                                      m.num_models, m.hyper[0], m.hyper[1], PE, G, pending);
+    {
+      const int cpb = m.tune.hier_cpb;
+      hier_nc_kernel<<<(npts + cpb - 1) / cpb, 32 * cpb, 0, st>>>(Q, npts, ld, m.y, m.sigma, m.offsets,
+                                                                  m.chains_per_model, m.num_models, m.hyper[0],
+                                                                  m.hyper[1], PE, G, pending);
+    }
       break;
     case 2: {
       if (m.precision == 1 && m.tc) return logreg_tc_launch(m, Q, npts, PE, G, pending, st);
@@ -484,31 +512,37 @@ cudaError_t launch_potential(ModelDev& m, const float* Q, int npts, double* PE, 
         cudaFuncSetAttribute(logreg_simt_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)logreg_smem(64));
         attr_set = true;
       }
-      dim3 grid((npts + LR_CT - 1) / LR_CT, m.row_groups);
-      logreg_simt_kernel<<<grid, 256, sm, st>>>(m.x, m.y, m.n, m.p, DP, Q, npts, ld, m.part_g, m.part_ll,
-                                                m.row_groups, pending);
-      logreg_finish_kernel<<<(npts + 7) / 8, 256, 0, st>>>(Q, npts, ld, m.p, m.row_groups, m.part_g, m.part_ll,
-                                                           nullptr, m.hyper[0], PE, G, pending);
+      const int rg = m.tune.lr_rg > 0 ? m.tune.lr_rg : m.row_groups;
+      dim3 grid((npts + LR_CT - 1) / LR_CT, rg);
+      logreg_simt_kernel<<<grid, 256, sm, st>>>(m.x, m.y, m.n, m.p, DP, Q, npts, ld, m.part_g, m.part_ll, rg,
+                                                pending);
+      logreg_finish_kernel<<<(npts + 7) / 8, 256, 0, st>>>(Q, npts, ld, m.p, rg, m.part_g, m.part_ll, nullptr,
+                                                           m.hyper[0], PE, G, pending);
       break;
     }
     case 3: {
       const int P = m.p, M = (int)m.n, cp = pad4(npts), pp = pad4(P);
-      const int mt = (M + HS_BM - 1) / HS_BM;
+      const int tm = m.tune.hs_tm, splits = m.tune.hs_splits, bm = 16 * tm;
+      const int mt = (M + bm - 1) / bm;
       // beta^T for the chains' query points
       dim3 gp((cp + 31) / 32, (pp + 31) / 32);
       const int nc = m.hyper[0] != 0.0;
       hs_pack_kernel<<<gp, 256, 0, st>>>(Q, ld, npts, P, nc, m.hs_bt, cp, pp, pending);
       // R[row][c] = y[row] - sum_p X[row][p] beta_c[p]
       dim3 g1((npts + HS_BN - 1) / HS_BN, mt, 1);
-      hs_sgemm_nn_kernel<<<g1, 256, 0, st>>>(m.hs_xt, pad4(M), m.hs_bt, cp, M, npts, P, P, m.resid, cp, 0, m.y,
-                                             m.part_rr, cp, pending);
+      if (tm == 2)
+        hs_sgemm_nn_kernel<2><<<g1, 256, 0, st>>>(m.hs_xt, pad4(M), m.hs_bt, cp, M, npts, P, P, m.resid, cp, 0,
+                                                  m.y, m.part_rr, cp, pending);
+      else
+        hs_sgemm_nn_kernel<4><<<g1, 256, 0, st>>>(m.hs_xt, pad4(M), m.hs_bt, cp, M, npts, P, P, m.resid, cp, 0,
+                                                  m.y, m.part_rr, cp, pending);
       // GB[s][c][p] = sum_{row in split s} R[row][c] X[row][p]
-      const int kps = (((M + HS_SPLITS - 1) / HS_SPLITS) + HS_BK - 1) / HS_BK * HS_BK;
-      dim3 g2((P + HS_BN - 1) / HS_BN, (npts + HS_BM - 1) / HS_BM, HS_SPLITS);
-      hs_sgemm_nn_kernel<<<g2, 256, 0, st>>>(m.resid, cp, m.hs_xp, pp, npts, P, M, kps, m.part_gb, pp,
-                                             (int64_t)npts * pp, nullptr, nullptr, 0, pending);
-      horseshoe_finish_kernel<<<npts, 256, 0, st>>>(Q, npts, ld, P, m.n, m.part_gb, HS_SPLITS, pp, m.part_rr, cp,
-                                                    mt, nc, PE, G, pending);
+      const int kps = (((M + splits - 1) / splits) + HS_BK - 1) / HS_BK * HS_BK;
+      dim3 g2((P + HS_BN - 1) / HS_BN, (npts + 63) / 64, splits);
+      hs_sgemm_nn_kernel<4><<<g2, 256, 0, st>>>(m.resid, cp, m.hs_xp, pp, npts, P, M, kps, m.part_gb, pp,
+                                                (int64_t)npts * pp, nullptr, nullptr, 0, pending);
+      horseshoe_finish_kernel<<<npts, 256, 0, st>>>(Q, npts, ld, P, m.n, m.part_gb, splits, pp, m.part_rr, cp, mt,
+                                                    nc, PE, G, pending);
       break;
     }
     case 4:
@@ -519,6 +553,111 @@ cudaError_t launch_potential(ModelDev& m, const float* Q, int npts, double* PE, 
       return cudaErrorInvalidValue;
   }
   return cudaGetLastError();
+}
+
+// ============================================================ autotuner
+namespace {
+std::mutex g_tune_mu;
+std::map<std::string, TuneParams> g_tune_cache;
+
+// mean CUDA-event time of one potential launch (after one untimed launch)
+cudaError_t time_potential(ModelDev& m, const float* Q, int npts, double* PE, float* G, cudaStream_t st, int reps,
+                           float* ms) {
+  cudaEvent_t a = nullptr, b = nullptr;
+  cudaError_t e = cudaEventCreate(&a);
+  if (e == cudaSuccess) e = cudaEventCreate(&b);
+  if (e == cudaSuccess) e = launch_potential(m, Q, npts, PE, G, nullptr, st);
+  if (e == cudaSuccess) e = cudaEventRecord(a, st);
+  for (int r = 0; r < reps && e == cudaSuccess; ++r) e = launch_potential(m, Q, npts, PE, G, nullptr, st);
+  if (e == cudaSuccess) e = cudaEventRecord(b, st);
+  if (e == cudaSuccess) e = cudaEventSynchronize(b);
+  float t = 0.0f;
+  if (e == cudaSuccess) e = cudaEventElapsedTime(&t, a, b);
+  *ms = t / (float)reps;
+  if (a) cudaEventDestroy(a);
+  if (b) cudaEventDestroy(b);
+  return e;
+}
+
+std::string tune_report(const ModelDev& m) {
+  char buf[160];
+  switch (m.family) {
+    case 1: snprintf(buf, sizeof(buf), "hier_chains_per_cta=%d", m.tune.hier_cpb); break;
+    case 2:
+      snprintf(buf, sizeof(buf), "logreg_row_groups=%d", m.tune.lr_rg > 0 ? m.tune.lr_rg : m.row_groups);
+      break;
+    case 3:
+      snprintf(buf, sizeof(buf), "horseshoe_tile_rows=%d horseshoe_splits=%d", 16 * m.tune.hs_tm,
+               m.tune.hs_splits);
+      break;
+    default: buf[0] = 0; break;
+  }
+  return std::string(buf);
+}
+}  // namespace
+
+cudaError_t autotune_potential(ModelDev& m, const float* Q, int npts, double* PE, float* G, cudaStream_t st,
+                               std::string* report) {
+  int dev = 0;
+  cudaGetDevice(&dev);
+  char key[192];
+  snprintf(key, sizeof(key), "%d|%d|%lld|%d|%d|%d|%d|%d|%g", dev, m.family, (long long)m.n, m.p, m.D, m.num_models,
+           npts, m.precision, m.hyper[0]);
+  std::lock_guard<std::mutex> lock(g_tune_mu);
+  auto it = g_tune_cache.find(key);
+  cudaError_t e = ensure_potential_scratch(m, npts);
+  if (e != cudaSuccess) return e;
+  const char* forced = getenv("GBN_TUNE");  // "hier_cpb=16 hs_tm=2 hs_splits=8 lr_rg=32": fixed shapes
+  if (forced && forced[0]) {
+    int v = 0;
+    const char* p;
+    if ((p = strstr(forced, "hier_cpb=")) && sscanf(p + 9, "%d", &v) == 1 && (v == 4 || v == 8 || v == 16))
+      m.tune.hier_cpb = v;
+    if ((p = strstr(forced, "hs_tm=")) && sscanf(p + 6, "%d", &v) == 1 && (v == 2 || v == 4)) m.tune.hs_tm = v;
+    if ((p = strstr(forced, "hs_splits=")) && sscanf(p + 10, "%d", &v) == 1 && v >= 1 && v <= HS_MAX_SPLITS)
+      m.tune.hs_splits = v;
+    if ((p = strstr(forced, "lr_rg=")) && sscanf(p + 6, "%d", &v) == 1 && v >= 1 && v <= m.row_groups_cap)
+      m.tune.lr_rg = v;
+  } else if (it != g_tune_cache.end()) {
+    m.tune = it->second;
+  } else {
+    std::vector<TuneParams> cand;
+    TuneParams t = m.tune;
+    if (m.family == 1) {
+      for (int cpb : {4, 8, 16}) {
+        t.hier_cpb = cpb;
+        cand.push_back(t);
+      }
+    } else if (m.family == 2 && !(m.precision == 1 && m.tc)) {
+      for (int rg : {std::max(1, m.row_groups / 2), m.row_groups, m.row_groups_cap}) {
+        t.lr_rg = rg;
+        cand.push_back(t);
+      }
+    } else if (m.family == 3) {
+      for (int tm : {2, 4})
+        for (int sp : {2, 4, 8}) {
+          t.hs_tm = tm;
+          t.hs_splits = sp;
+          cand.push_back(t);
+        }
+    }
+    float best = 1e30f;
+    TuneParams pick = m.tune;
+    for (const TuneParams& c : cand) {
+      m.tune = c;
+      float ms = 0.0f;
+      e = time_potential(m, Q, npts, PE, G, st, 3, &ms);
+      if (e != cudaSuccess) return e;
+      if (ms < best) {
+        best = ms;
+        pick = c;
+      }
+    }
+    m.tune = pick;
+    g_tune_cache[key] = pick;
+  }
+  if (report) *report = tune_report(m);
+  return cudaSuccess;
 }
 
 cudaError_t launch_scale_rows(const double* cot, float* G, int npts, int D, cudaStream_t st) {

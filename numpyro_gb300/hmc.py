@@ -201,6 +201,13 @@ class HMC(MCMCKernel):
         except Exception:
             pass
 
+    def tuning(self):
+        """Launch shapes the autotuner chose for this kernel's potential (gbn_tuning)."""
+        if self._handle is None:
+            return ""
+        v = _lib.load().gbn_tuning(self._handle)
+        return v.decode() if v else ""
+
     @property
     def num_chains(self):
         return self._handle_key[0] if self._handle_key else None

@@ -128,3 +128,37 @@ def test_logreg_tc_matches_fp32_path_full_size():
     assert abs(pe_tc[5] - pr) <= 2e-8 * abs(pr) + 0.05
     ktc.close()
     k32.close()
+
+
+TUNED = [c for c in CASES if c[0] in ("hier_nc", "logreg", "horseshoe", "horseshoe_nc")]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", TUNED, ids=[c[0] for c in TUNED])
+def test_autotuner_reports_its_choice(case):
+    name, model, _ = case
+    k = NUTS(model, num_chains=16)
+    k.potential_and_grad(torch.as_tensor(typical_points(name, model, np.random.default_rng(0), 16), device="cuda"))
+    assert "=" in k.tuning(), k.tuning()
+    k.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("shape", ["hs_tm=2 hs_splits=1", "hs_tm=2 hs_splits=8", "hs_tm=4 hs_splits=3"])
+@pytest.mark.parametrize("name", ["horseshoe", "horseshoe_nc"])
+def test_horseshoe_tile_shapes_agree_with_oracle(shape, name, monkeypatch):
+    """Every tile height / split count the autotuner may pick gives the oracle's potential."""
+    monkeypatch.setenv("GBN_TUNE", shape)
+    _, model, ref = [c for c in CASES if c[0] == name][0]
+    rng = np.random.default_rng(2)
+    C = 21
+    z = typical_points(name, model, rng, C)
+    k = NUTS(model, num_chains=C)
+    pe, g = k.potential_and_grad(torch.as_tensor(z, device="cuda"))
+    assert k.tuning() == "horseshoe_tile_rows=%d horseshoe_splits=%d" % (16 * int(shape[6]), int(shape.split("=")[-1]))
+    pe, g = pe.cpu().numpy(), g.cpu().numpy()
+    for c in range(C):
+        pr, gr = ref(z[c].astype(np.float64))
+        assert abs(pe[c] - pr) <= 2e-6 * max(1.0, abs(pr)), (shape, c, pe[c], pr)
+        np.testing.assert_allclose(g[c], gr, atol=1e-3 * max(1.0, np.max(np.abs(gr))), rtol=1e-3)
+    k.close()
