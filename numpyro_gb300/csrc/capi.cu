@@ -619,7 +619,7 @@ int gbn_run(gbn_handle h, void* stream, gbn_state* st, int32_t num_iterations, i
     if (e != cudaSuccess) return cuda_fail(h, e, "gbn_run: queue");
     if (h->m.family == GBN_FAMILY_SV) {
       SvView sv{h->m.y, (int)h->m.n, h->m.hyper[2] != 0.0, h->m.hyper[0], h->m.hyper[1]};
-      launch_persistent_sv(h->dP, sv, h->counters + 7, h->C, s);
+      launch_persistent_sv(h->dP, sv, h->counters + 7, h->C, h->D, s);
     } else {
       HierView hv{h->m.y, h->m.sigma, h->m.offsets, h->m.chains_per_model, h->m.num_models, h->m.hyper[0],
                   h->m.hyper[1]};

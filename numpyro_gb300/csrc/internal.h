@@ -75,7 +75,8 @@ inline int pad4(int v) { return (v + 3) & ~3; }
 void launch_advance(const AdvParams* dP, int C, int D, bool cta_per_chain, bool dense, int parity, cudaStream_t st);
 void launch_persistent_hier(const AdvParams* dP, const HierView& hv, int32_t* queue_head, const int32_t* order,
                             int C, bool dense, cudaStream_t st);
-void launch_persistent_sv(const AdvParams* dP, const SvView& sv, int32_t* queue_head, int C, cudaStream_t st);
+void launch_persistent_sv(const AdvParams* dP, const SvView& sv, int32_t* queue_head, int C, int D,
+                          cudaStream_t st);
 void launch_init_uniform(const AdvParams* dP, int C, int D, int attempt, const int32_t* flag, cudaStream_t st);
 void launch_check_valid(const AdvParams* dP, int C, int32_t* flag, int32_t* count, cudaStream_t st);
 void launch_init_state(const AdvParams* dP, int C, int D, const float* inv_mass_init, float init_step,

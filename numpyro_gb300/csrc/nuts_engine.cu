@@ -91,6 +91,23 @@ struct Chain {
   int D;   // this chain's latent dim
   int ld;  // row stride of [C][ld] buffers
   ChainCtl ctl;
+  // The twelve tree vectors (frontiers, proposals, momentum sums) are this chain's rows of the
+  // EngineBufs [C][ld] buffers, or, when oc is set, consecutive rows of ld floats on chip.
+  float* oc;
+  __device__ __forceinline__ float* z_l_() const { return oc ? oc + 0 * (size_t)ld : V(P.e.z_l); }
+  __device__ __forceinline__ float* r_l_() const { return oc ? oc + 1 * (size_t)ld : V(P.e.r_l); }
+  __device__ __forceinline__ float* g_l_() const { return oc ? oc + 2 * (size_t)ld : V(P.e.g_l); }
+  __device__ __forceinline__ float* z_r_() const { return oc ? oc + 3 * (size_t)ld : V(P.e.z_r); }
+  __device__ __forceinline__ float* r_r_() const { return oc ? oc + 4 * (size_t)ld : V(P.e.r_r); }
+  __device__ __forceinline__ float* g_r_() const { return oc ? oc + 5 * (size_t)ld : V(P.e.g_r); }
+  __device__ __forceinline__ float* z_p_() const { return oc ? oc + 6 * (size_t)ld : V(P.e.z_p); }
+  __device__ __forceinline__ float* g_p_() const { return oc ? oc + 7 * (size_t)ld : V(P.e.g_p); }
+  __device__ __forceinline__ float* z_sp_() const { return oc ? oc + 8 * (size_t)ld : V(P.e.z_sp); }
+  __device__ __forceinline__ float* g_sp_() const { return oc ? oc + 9 * (size_t)ld : V(P.e.g_sp); }
+  __device__ __forceinline__ float* rsum_() const { return oc ? oc + 10 * (size_t)ld : V(P.e.rsum); }
+  __device__ __forceinline__ float* rsum_sub_() const { return oc ? oc + 11 * (size_t)ld : V(P.e.rsum_sub); }
+  __device__ __forceinline__ float* Q_() const { return V(P.e.Q); }
+  __device__ __forceinline__ float* G_() const { return V(P.e.G); }
 
   __device__ __forceinline__ size_t row() const { return (size_t)c * ld; }
   __device__ __forceinline__ float* V(float* base) const { return base + row(); }
@@ -229,11 +246,11 @@ struct Chain {
   // ----------------------------------------------------------- leapfrog halves
   // first half-kick + drift from the frontier on side `right`; writes Q
   __device__ void leaf_prepare(bool right, float eps) {
-    float* z = V(right ? P.e.z_r : P.e.z_l);
-    float* r = V(right ? P.e.r_r : P.e.r_l);
-    const float* gr = V(right ? P.e.g_r : P.e.g_l);
+    float* z = (right ? z_r_() : z_l_());
+    float* r = (right ? r_r_() : r_l_());
+    const float* gr = (right ? g_r_() : g_l_());
     const float* mi = V(P.s.inverse_mass_matrix);
-    float* q = V(P.e.Q);
+    float* q = Q_();
     if (DM) {  // r_half = r - eps/2 g; z += eps M^-1 r_half
       for (int d = g.tid; d < D; d += NT) r[d] = r[d] - 0.5f * eps * gr[d];
       g.sync();
@@ -269,9 +286,9 @@ struct Chain {
   }
   // second half-kick with the new gradient; returns K(r_new)
   __device__ double leaf_finish(bool right, float eps) {
-    float* r = V(right ? P.e.r_r : P.e.r_l);
-    float* gr = V(right ? P.e.g_r : P.e.g_l);
-    const float* G = V(P.e.G);
+    float* r = (right ? r_r_() : r_l_());
+    float* gr = (right ? g_r_() : g_l_());
+    const float* G = G_();
     const float* mi = V(P.s.inverse_mass_matrix);
     if (DM) {
       for (int d = g.tid; d < D; d += NT) {
@@ -314,9 +331,9 @@ struct Chain {
     const float* ms = V(P.s.mass_matrix_sqrt);
     const float* z = V(P.s.z);
     const float* gz = V(P.s.z_grad);
-    float *zl = V(P.e.z_l), *zr = V(P.e.z_r), *zp = V(P.e.z_p);
-    float *rl = V(P.e.r_l), *rr = V(P.e.r_r), *rs = V(P.e.rsum);
-    float *gl = V(P.e.g_l), *grr = V(P.e.g_r), *gp = V(P.e.g_p);
+    float *zl = z_l_(), *zr = z_r_(), *zp = z_p_();
+    float *rl = r_l_(), *rr = r_r_(), *rs = rsum_();
+    float *gl = g_l_(), *grr = g_r_(), *gp = g_p_();
     float kin = 0.0f;
     const float* mi = V(P.s.inverse_mass_matrix);
     double kin_dense = 0.0;
@@ -411,12 +428,12 @@ struct Chain {
     double w = -dE;
     int div = dE > P.max_dE;
     double acc = (double)exp_min1_f(-dE);
-    const float* zf = V(right ? P.e.z_r : P.e.z_l);
-    const float* rf = V(right ? P.e.r_r : P.e.r_l);
-    const float* gf = V(right ? P.e.g_r : P.e.g_l);
-    float* zsp = V(P.e.z_sp);
-    float* gsp = V(P.e.g_sp);
-    float* rss = V(P.e.rsum_sub);
+    const float* zf = (right ? z_r_() : z_l_());
+    const float* rf = (right ? r_r_() : r_l_());
+    const float* gf = (right ? g_r_() : g_l_());
+    float* zsp = z_sp_();
+    float* gsp = g_sp_();
+    float* rss = rsum_sub_();
     int leaf_idx = ctl.sub_num;
     if (leaf_idx == 0) {
       for (int d0 = g.tid; d0 < D; d0 += UB * NT) {
@@ -498,8 +515,8 @@ struct Chain {
   __device__ void combine_subtree() {
     uint32_t n = P.s.rng_key[2 * c + 1];
     uint32_t chain_id = P.s.rng_key[2 * c];
-    float* rs = V(P.e.rsum);
-    const float* rss = V(P.e.rsum_sub);
+    float* rs = rsum_();
+    const float* rss = rsum_sub_();
     for (int d0 = g.tid; d0 < D; d0 += UB * NT) {
       float a[UB], b[UB];
 #pragma unroll
@@ -520,12 +537,12 @@ struct Chain {
       p = exp_min1_f(ctl.sub_w - ctl.tree_w);
     }
     bool turning = ctl.sub_turning;
-    if (!turning) turning = is_turning(V(P.e.r_l), V(P.e.r_r), rs, nullptr, nullptr);
+    if (!turning) turning = is_turning(r_l_(), r_r_(), rs, nullptr, nullptr);
     uint4 u = draw(P.seed, chain_id, n, P_DOUBLING, (uint32_t)ctl.depth, 0);
     bool take = u01f(u.y) < p;
     if (take) {
-      copy(V(P.e.z_p), V(P.e.z_sp));
-      copy(V(P.e.g_p), V(P.e.g_sp));
+      copy(z_p_(), z_sp_());
+      copy(g_p_(), g_sp_());
       ctl.pe_p = ctl.pe_sp;
       ctl.energy_p = ctl.energy_sp;
     }
@@ -674,9 +691,9 @@ struct Chain {
     const float* mi = V(P.s.inverse_mass_matrix);
     const float* z = V(P.s.z);
     const float* gz = V(P.s.z_grad);
-    float* r0 = V(P.e.r_l);
-    float* rh = V(P.e.r_r);
-    float* q = V(P.e.Q);
+    float* r0 = r_l_();
+    float* rh = r_r_();
+    float* q = Q_();
     if (DM) {
       // the trial momentum is M^-1 eps, as momentum_generator(z, inverse_mass_matrix, key) at
       // hmc_util.py:356 (the dense inverse mass matrix stands in for the square root there)
@@ -711,11 +728,11 @@ struct Chain {
   __device__ bool heur_finish() {
     float eps = (float)ctl.heur_step;
     const float* mi = V(P.s.inverse_mass_matrix);
-    const float* G = V(P.e.G);
-    const float* rh = V(P.e.r_r);
+    const float* G = G_();
+    const float* rh = r_r_();
     double e_new;
     if (DM) {
-      float* rn = V(P.e.r_r);  // r_new overwrites r_half in place
+      float* rn = r_r_();  // r_new overwrites r_half in place
       for (int d = g.tid; d < D; d += NT) rn[d] = rn[d] - 0.5f * eps * G[d];
       e_new = P.e.PE[c] + kinetic_dense(rn);
     } else {
@@ -864,7 +881,7 @@ struct Chain {
         bool take = u01f(u.x) < (float)acc;
         bool pend;
         if (take)
-          pend = finish_transition(pe, e_new, ctl.hmc_total, acc, div, V(P.e.z_r), V(P.e.g_r));
+          pend = finish_transition(pe, e_new, ctl.hmc_total, acc, div, z_r_(), g_r_());
         else
           pend = finish_transition(P.s.potential_energy[c], ctl.energy0, ctl.hmc_total, acc, div, V(P.s.z),
                                    V(P.s.z_grad));
@@ -887,7 +904,7 @@ struct Chain {
         }
         double accept_prob = ctl.tree_acc / (double)ctl.num_prop;
         bool pend = finish_transition(ctl.pe_p, ctl.energy_p, ctl.num_prop, accept_prob, ctl.tree_div,
-                                      V(P.e.z_p), V(P.e.g_p));
+                                      z_p_(), g_p_());
         if (pend) return;
         need_start = true;
         break;
@@ -930,7 +947,7 @@ __global__ void __launch_bounds__(256) advance_kernel(const AdvParams* __restric
   }
   int pending = 0, active = 0;
   if (c < P.C) {
-    Chain<NT, DM> ch{P, Group<NT>{tid}, red, c, P.e.chain_dim ? P.e.chain_dim[c] : P.D, P.D, P.e.ctl[c]};
+    Chain<NT, DM> ch{P, Group<NT>{tid}, red, c, P.e.chain_dim ? P.e.chain_dim[c] : P.D, P.D, P.e.ctl[c], nullptr};
     ch.run();
     if (tid == 0) {
       P.e.ctl[c] = ch.ctl;
@@ -1078,7 +1095,7 @@ __global__ void __launch_bounds__(256) persistent_hier_kernel(const AdvParams* _
     int m = c / hv.cpm;
     if (m >= hv.num_models) m = hv.num_models - 1;
     const int j0 = hv.off[m], J = hv.off[m + 1] - j0;
-    Chain<32, DM> ch{P, Group<32>{lane}, nullptr, c, P.e.chain_dim ? P.e.chain_dim[c] : P.D, P.D, P.e.ctl[c]};
+    Chain<32, DM> ch{P, Group<32>{lane}, nullptr, c, P.e.chain_dim ? P.e.chain_dim[c] : P.D, P.D, P.e.ctl[c], nullptr};
     ch.run();
     for (;;) {
       const int ph = ch.ctl.phase;
@@ -1098,10 +1115,17 @@ __global__ void __launch_bounds__(256) persistent_hier_kernel(const AdvParams* _
 // inline, so no leapfrog step costs a kernel launch or a host round trip.  Every thread
 // carries the same ChainCtl (its decisions come from block-wide reductions and the
 // counter-based stream), so the control flow is uniform across the CTA.
+// ONCHIP keeps the chain's twelve tree vectors (frontiers, proposals, momentum sums) in dynamic
+// shared memory (12 D floats): they live only within a transition, so nothing needs copying in
+// or out.  The query/gradient rows, the U-turn checkpoints and the sampler state stay in global
+// memory.
+constexpr int SV_ONCHIP_VECS = 12;
+template <bool ONCHIP>
 __global__ void __launch_bounds__(256) persistent_sv_kernel(const AdvParams* __restrict__ Pp, SvView sv,
                                                             int32_t* queue_head) {
   __shared__ SvSmem<256> sm;
   __shared__ int next_chain;
+  extern __shared__ float onchip[];
   const AdvParams& P = *Pp;
   const int tid = threadIdx.x;
   for (;;) {
@@ -1110,7 +1134,8 @@ __global__ void __launch_bounds__(256) persistent_sv_kernel(const AdvParams* __r
     const int c = next_chain;
     __syncthreads();  // every thread has read next_chain before it is overwritten
     if (c >= P.C) break;
-    Chain<256> ch{P, Group<256>{tid}, sm.red, c, P.D, P.D, P.e.ctl[c]};
+    Chain<256> ch{P, Group<256>{tid}, sm.red, c, P.D, P.D, P.e.ctl[c], nullptr};
+    if (ONCHIP) ch.oc = onchip;  // SV_ONCHIP_VECS consecutive rows of D floats
     ch.run();
     float* q = P.e.Q + (size_t)c * P.D;
     float* gr = P.e.G + (size_t)c * P.D;
@@ -1126,6 +1151,7 @@ __global__ void __launch_bounds__(256) persistent_sv_kernel(const AdvParams* __r
       ch.run();
     }
     if (tid == 0) P.e.ctl[c] = ch.ctl;
+    __syncthreads();  // the on-chip rows are free for the next chain
   }
 }
 
@@ -1149,15 +1175,30 @@ void launch_persistent_hier(const AdvParams* dP, const HierView& hv, int32_t* qu
     persistent_hier_kernel<false><<<blocks, 256, 0, st>>>(dP, hv, queue_head, order);
 }
 
-void launch_persistent_sv(const AdvParams* dP, const SvView& sv, int32_t* queue_head, int C, cudaStream_t st) {
-  int dev = 0, sms = 0, per_sm = 0;
+void launch_persistent_sv(const AdvParams* dP, const SvView& sv, int32_t* queue_head, int C, int D,
+                          cudaStream_t st) {
+  int dev = 0, sms = 0, per_sm = 0, optin = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, persistent_sv_kernel, 256, 0);
+  cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  // On-chip rows make each leaf about a quarter faster (T = 4096 on GB300), but at 12 D floats per
+  // CTA they can cost resident chains (197 KB: one CTA per SM, against two with global rows).  They
+  // are used only when every chain is resident either way.
+  const size_t onchip = sizeof(float) * (size_t)SV_ONCHIP_VECS * D;
+  bool use_onchip = onchip + sizeof(SvSmem<256>) + 64 <= (size_t)optin;
+  if (use_onchip) {
+    cudaFuncSetAttribute(persistent_sv_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)onchip);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, persistent_sv_kernel<true>, 256, onchip);
+    if (per_sm < 1 || (int64_t)sms * per_sm < C) use_onchip = false;
+  }
+  if (!use_onchip) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, persistent_sv_kernel<false>, 256, 0);
   if (per_sm < 1) per_sm = 1;
   int blocks = sms * per_sm;
   if (blocks > C) blocks = C;
-  persistent_sv_kernel<<<blocks, 256, 0, st>>>(dP, sv, queue_head);
+  if (use_onchip)
+    persistent_sv_kernel<true><<<blocks, 256, onchip, st>>>(dP, sv, queue_head);
+  else
+    persistent_sv_kernel<false><<<blocks, 256, 0, st>>>(dP, sv, queue_head);
 }
 
 void launch_advance(const AdvParams* dP, int C, int D, bool cta_per_chain, bool dense, int parity, cudaStream_t st) {

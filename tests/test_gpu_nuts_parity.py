@@ -3,7 +3,7 @@
 Each GPU transition is replayed by the oracle from the GPU's own starting
 state (so FP32-vs-FP64 chaos cannot accumulate), with the same stream
 addresses.  Tree sizes (num_steps) must agree on >= 99.9% of transitions,
-positions within 1e-5 relative on trajectories that take the same decisions.
+positions within 1e-5 relative (median) on trajectories that take the same decisions.
 """
 import numpy as np
 import pytest
@@ -63,7 +63,7 @@ def test_single_transition_parity(engine):
     state.adapt_state.inverse_mass_matrix.copy_(inv)
     state.adapt_state.mass_matrix_sqrt.copy_(1.0 / inv.sqrt())
     same, total, zerr = 0, 0, []
-    for it in range(6):
+    for it in range(8):
         z0 = state.z.cpu().numpy().copy()
         new = k.sample(state)
         zg = new.z.cpu().numpy()
@@ -79,7 +79,8 @@ def test_single_transition_parity(engine):
                 zerr.append(np.max(np.abs(ref.z - zg[c]) / (np.abs(ref.z) + 1e-2)))
         state = new
     frac = same / total
-    assert frac >= 0.99, frac
+    print("tree sizes identical on %d of %d transitions (%.4f)" % (same, total, frac))
+    assert frac >= 0.999, frac  # 2048 transitions: at most 2 may part
     assert np.median(zerr) < 1e-5, np.median(zerr)
     k.close()
 
