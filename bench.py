@@ -86,7 +86,10 @@ def run_workload(args):
         W = args.num_warmup
     if args.samples:
         S = args.samples
-    k = NUTS(model, num_chains=C)
+    kw = {"precision": args.precision} if args.precision else {}
+    k = NUTS(model, num_chains=C, **kw)
+    if args.precision:
+        shape += ", precision " + args.precision
     log("%s: %s, %d warmup + %d samples" % (w, shape, W, S))
     st = k.init(1, W)
     ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]

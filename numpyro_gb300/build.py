@@ -19,7 +19,7 @@ INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall",
               "--expt-relaxed-constexpr", "-I", CSRC, "-I", INCLUDE]
-SOURCES = ["nuts_engine.cu", "potentials_simt.cu", "logreg_tc.cu", "capi.cu", "noalloc.cu"]
+SOURCES = ["nuts_engine.cu", "potentials_simt.cu", "logreg_tc.cu", "horseshoe_tc.cu", "capi.cu", "noalloc.cu"]
 
 
 def nvcc():

@@ -159,6 +159,7 @@ int gbn_destroy(gbn_handle h) {
   if (!h) return GBN_OK;
   cudaDeviceSynchronize();
   if (h->m.tc) logreg_tc_free(h->m);
+  if (h->m.hs_tc) horseshoe_tc_free(h->m);
   free_potential_scratch(h->m);
   for (void* p : h->allocs) cudaFree(p);
   if (h->h_counters) cudaFreeHost(h->h_counters);
@@ -349,6 +350,13 @@ int gbn_create(gbn_handle* out, const gbn_model_desc* md, const gbn_config* cfg)
                   "bf16x3 needs a design matrix exactly representable in bfloat16 (use precision fp32)");
     }
   }
+  if (ce == cudaSuccess && m.family == GBN_FAMILY_HORSESHOE && m.precision == GBN_PREC_BF16X3) {
+    if (!horseshoe_tc_supported(m)) {
+      gbn_destroy(h);
+      return fail(nullptr, GBN_ERR_UNSUPPORTED, "bf16x3 tensor-core horseshoe path unavailable on this GPU");
+    }
+    ce = horseshoe_tc_prepare(m, C);
+  }
   if (ce == cudaSuccess) ce = ensure_potential_scratch(m, C);
   if (ce != cudaSuccess) {
     int r = cuda_fail(nullptr, ce, "gbn_create: allocation");
@@ -485,7 +493,7 @@ static int tick_loop(gbn_handle h, cudaStream_t st, int64_t max_ticks) {
     e = cudaMemcpyAsync(h->h_counters, h->counters, sizeof(int32_t) * 4, cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return cuda_fail(h, e, "tick loop");
-    if (h->m.tc && logreg_tc_error(h->m))
+    if ((h->m.tc && logreg_tc_error(h->m)) || (h->m.hs_tc && horseshoe_tc_error(h->m)))
       return fail(h, GBN_ERR_TIMEOUT, "tensor-core potential: a device wait timed out");
     if (h->h_counters[2 * last + 1] == 0) break;
     if (ticks > max_ticks) return fail(h, GBN_ERR_TIMEOUT, "tick budget exhausted: chains did not finish");

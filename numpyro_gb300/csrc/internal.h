@@ -48,6 +48,7 @@ struct ModelDev {
   float* hs_xt = nullptr;
   float* hs_xp = nullptr;
   float* hs_bt = nullptr;
+  void* hs_tc = nullptr;  // horseshoe tensor-core path state (horseshoe_tc.cu)
 };
 
 // device view of the hierarchical family's data (persistent engine)
@@ -98,6 +99,14 @@ cudaError_t autotune_potential(ModelDev& m, const float* Q, int npts, double* PE
                                std::string* report);
 // VJP: out[k] = cot[k] * grad U(z_k)
 cudaError_t launch_scale_rows(const double* cot, float* G, int npts, int D, cudaStream_t st);
+
+// horseshoe_tc.cu (tensor-core bf16x3 GEMMs of the horseshoe potential)
+bool horseshoe_tc_supported(const ModelDev& m);
+cudaError_t horseshoe_tc_prepare(ModelDev& m, int points);
+void horseshoe_tc_free(ModelDev& m);
+int horseshoe_tc_error(const ModelDev& m);  // nonzero: a device wait timed out
+cudaError_t horseshoe_tc_launch(ModelDev& m, const float* Q, int npts, double* PE, float* G, const int32_t* pending,
+                                cudaStream_t st);
 
 // logreg_tc.cu (tensor-core BF16 split-precision logistic potential)
 bool logreg_tc_supported(const ModelDev& m);

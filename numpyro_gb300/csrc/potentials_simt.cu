@@ -521,6 +521,7 @@ cudaError_t launch_potential(ModelDev& m, const float* Q, int npts, double* PE, 
       break;
     }
     case 3: {
+      if (m.precision == 1 && m.hs_tc) return horseshoe_tc_launch(m, Q, npts, PE, G, pending, st);
       const int P = m.p, M = (int)m.n, cp = pad4(npts), pp = pad4(P);
       const int tm = m.tune.hs_tm, splits = m.tune.hs_splits, bm = 16 * tm;
       const int mt = (M + bm - 1) / bm;
@@ -691,6 +692,13 @@ cudaError_t launch_logreg_simt_scratch(const float* x, const float* y, int64_t n
   logreg_finish_kernel<<<(npts + 7) / 8, 256, 0, st>>>(Q, npts, p, p, row_groups, part_g, part_ll, nullptr,
                                                        prior_scale, PE, G, nullptr);
   return cudaGetLastError();
+}
+
+void horseshoe_finish_launch(const float* Q, int npts, int ld, int P, int64_t N, const float* part_gb, int splits,
+                             int ldg, const double* part_rr, int ld_rr, int mtiles, int noncentred, double* PE,
+                             float* G, const int32_t* pending, cudaStream_t st) {
+  horseshoe_finish_kernel<<<npts, 256, 0, st>>>(Q, npts, ld, P, N, part_gb, splits, ldg, part_rr, ld_rr, mtiles,
+                                                noncentred, PE, G, pending);
 }
 
 void logreg_finish_launch(const float* Q, int npts, int ld, int p, int row_groups, const float* part_g,

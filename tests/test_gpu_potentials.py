@@ -162,3 +162,28 @@ def test_horseshoe_tile_shapes_agree_with_oracle(shape, name, monkeypatch):
         assert abs(pe[c] - pr) <= 2e-6 * max(1.0, abs(pr)), (shape, c, pe[c], pr)
         np.testing.assert_allclose(g[c], gr, atol=1e-3 * max(1.0, np.max(np.abs(gr))), rtol=1e-3)
     k.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("noncentered", [False, True])
+@pytest.mark.parametrize("shape", [(200, 50, 37), (333, 130, 130)])
+def test_horseshoe_tensor_core_vs_oracle(shape, noncentered):
+    """precision="bf16x3": both horseshoe GEMMs on tcgen05 (six bf16 cross products per split
+    operand pair) match the FP64 oracle like the FP32 CUDA-core path."""
+    _tc_or_skip()
+    from numpyro_gb300 import datasets, models
+
+    n, p, C = shape
+    X, yh, _ = datasets.horseshoe_data(seed=9, n=n, p=p, nonzero=5)
+    model = models.HorseshoeRegression(X, yh, noncentered=noncentered)
+    name = "horseshoe_nc" if noncentered else "horseshoe"
+    ref = PR.make_potential(name, X.astype(np.float64), yh.astype(np.float64))
+    z = typical_points(name, model, np.random.default_rng(4), C)
+    k = NUTS(model, num_chains=C, precision="bf16x3")
+    pe, g = k.potential_and_grad(torch.as_tensor(z, device="cuda"))
+    pe, g = pe.cpu().numpy(), g.cpu().numpy()
+    for c in range(C):
+        pr, gr = ref(z[c].astype(np.float64))
+        assert abs(pe[c] - pr) <= 2e-6 * max(1.0, abs(pr)), (c, pe[c], pr)
+        np.testing.assert_allclose(g[c], gr, atol=1e-3 * max(1.0, np.max(np.abs(gr))), rtol=1e-3)
+    k.close()
