@@ -236,7 +236,7 @@ struct CollectBufs {  // mirrors gbn_collect
 
 // Everything the advance kernel needs; lives in device memory so captured
 // CUDA graphs stay valid when the caller's buffers change between calls.
-struct AdvParams {
+struct __align__(16) AdvParams {
   EngineBufs e;
   StateBufs s;
   CollectBufs col;

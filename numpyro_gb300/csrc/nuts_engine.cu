@@ -928,10 +928,23 @@ struct Chain {
   }
 };
 
+// The parameter block lives in device memory (so captured CUDA graphs stay valid when the
+// caller's buffers change between calls).  The state-machine kernels read its ~0.5 KB through
+// hundreds of dependent field loads; a CTA stages it in shared memory once instead.
+__device__ __forceinline__ const AdvParams& stage_params(const AdvParams* __restrict__ Pp, AdvParams* sp) {
+  static_assert(sizeof(AdvParams) % 16 == 0, "AdvParams is copied as 16-byte words");
+  const uint4* src = reinterpret_cast<const uint4*>(Pp);
+  uint4* dst = reinterpret_cast<uint4*>(sp);
+  for (int i = threadIdx.x; i < (int)(sizeof(AdvParams) / 16); i += blockDim.x) dst[i] = src[i];
+  __syncthreads();
+  return *sp;
+}
+
 template <int NT, bool DM>
 __global__ void __launch_bounds__(256) advance_kernel(const AdvParams* __restrict__ Pp, int parity) {
   __shared__ double red[16];
-  const AdvParams& P = *Pp;
+  __shared__ __align__(16) AdvParams sp;
+  const AdvParams& P = stage_params(Pp, &sp);
   int c;
   int tid;
   if (NT == 32) {
@@ -1084,7 +1097,8 @@ __global__ void set_rng_chain_kernel(uint32_t* rng_key, int C, int first_chain) 
 template <bool DM>
 __global__ void __launch_bounds__(256) persistent_hier_kernel(const AdvParams* __restrict__ Pp, HierView hv,
                                                               int32_t* queue_head, const int32_t* __restrict__ order) {
-  const AdvParams& P = *Pp;
+  __shared__ __align__(16) AdvParams sp;
+  const AdvParams& P = stage_params(Pp, &sp);
   const int lane = threadIdx.x & 31;
   for (;;) {
     int k = 0;
@@ -1125,8 +1139,9 @@ __global__ void __launch_bounds__(256) persistent_sv_kernel(const AdvParams* __r
                                                             int32_t* queue_head) {
   __shared__ SvSmem<256> sm;
   __shared__ int next_chain;
+  __shared__ __align__(16) AdvParams sp;
   extern __shared__ float onchip[];
-  const AdvParams& P = *Pp;
+  const AdvParams& P = stage_params(Pp, &sp);
   const int tid = threadIdx.x;
   for (;;) {
     if (tid == 0) next_chain = atomicAdd(queue_head, 1);
