@@ -231,6 +231,24 @@ int gbn_create(gbn_handle* out, const gbn_model_desc* md, const gbn_config* cfg)
       if (ce == cudaSuccess) ce = cudaMemcpy(m.sigma, md->sigma, sizeof(float) * md->n, cudaMemcpyHostToDevice);
       if (ce == cudaSuccess)
         ce = cudaMemcpy(m.offsets, md->offsets, sizeof(int32_t) * (m.num_models + 1), cudaMemcpyHostToDevice);
+      {
+        // 1/sigma per group and, per model, the constant of its potential (hier_potential.cuh)
+        const double LOG_2PI = 1.8378770664093453, LOG_PI = 1.1447298858494002, LOG_2 = 0.6931471805599453;
+        std::vector<float> sinv((size_t)md->n);
+        std::vector<double> cmodel((size_t)m.num_models);
+        for (int64_t j = 0; j < md->n; ++j) sinv[(size_t)j] = (float)(1.0 / (double)md->sigma[j]);
+        for (int k = 0; k < m.num_models; ++k) {
+          double c0 = 0.5 * LOG_2PI + log(m.hyper[0]) + LOG_PI + log(m.hyper[1]) - LOG_2;
+          for (int j = md->offsets[k]; j < md->offsets[k + 1]; ++j) c0 += log((double)md->sigma[j]) + LOG_2PI;
+          cmodel[(size_t)k] = c0;
+        }
+        if (ce == cudaSuccess) ce = dalloc(h, &m.hier_sinv, md->n);
+        if (ce == cudaSuccess) ce = dalloc(h, &m.hier_cmodel, (size_t)m.num_models);
+        if (ce == cudaSuccess)
+          ce = cudaMemcpy(m.hier_sinv, sinv.data(), sizeof(float) * sinv.size(), cudaMemcpyHostToDevice);
+        if (ce == cudaSuccess)
+          ce = cudaMemcpy(m.hier_cmodel, cmodel.data(), sizeof(double) * cmodel.size(), cudaMemcpyHostToDevice);
+      }
       break;
     }
     case GBN_FAMILY_LOGREG:
@@ -629,8 +647,8 @@ int gbn_run(gbn_handle h, void* stream, gbn_state* st, int32_t num_iterations, i
       SvView sv{h->m.y, (int)h->m.n, h->m.hyper[2] != 0.0, h->m.hyper[0], h->m.hyper[1]};
       launch_persistent_sv(h->dP, sv, h->counters + 7, h->C, h->D, s);
     } else {
-      HierView hv{h->m.y, h->m.sigma, h->m.offsets, h->m.chains_per_model, h->m.num_models, h->m.hyper[0],
-                  h->m.hyper[1]};
+      HierView hv{h->m.y, h->m.hier_sinv, h->m.hier_cmodel, h->m.offsets, h->m.chains_per_model, h->m.num_models,
+                  (float)(1.0 / (h->m.hyper[0] * h->m.hyper[0])), (float)(1.0 / h->m.hyper[1])};
       launch_persistent_hier(h->dP, hv, h->counters + 7, h->order, h->C, h->hp.dense != 0, s);
     }
     e = cudaGetLastError();

@@ -117,6 +117,8 @@ __device__ __forceinline__ FF ff_add(FF a, FF b) {
 }
 __device__ __forceinline__ FF ff_from(float x) { return FF{x, 0.0f}; }
 __device__ __forceinline__ double ff_value(FF a) { return (double)a.hi + (double)a.lo; }
+// hi + lo <= 0, decided exactly in FP32 (a renormalised pair has |lo| <= ulp(hi) / 2)
+__device__ __forceinline__ bool ff_le0(FF a) { return a.hi < 0.0f || (a.hi == 0.0f && a.lo <= 0.0f); }
 __device__ __forceinline__ FF ff_shfl_xor(FF v, int o) {
   return FF{__shfl_xor_sync(0xffffffffu, v.hi, o), __shfl_xor_sync(0xffffffffu, v.lo, o)};
 }

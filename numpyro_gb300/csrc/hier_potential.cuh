@@ -17,25 +17,35 @@
 
 namespace gbn {
 
-__device__ __forceinline__ void hier_nc_potential_warp(const float* z, float* g,
-                                                       double* __restrict__ pe_out, int J,
-                                                       const float* __restrict__ y, const float* __restrict__ sg,
-                                                       double mu_scale, double tau_scale, int lane) {
-  constexpr double LOG_2PI = 1.8378770664093453;
-  constexpr double LOG_PI = 1.1447298858494002;
-  constexpr double LOG_2 = 0.6931471805599453;
+// Per-model data of the hierarchical family: for each group y_j and 1/sigma_j; for each model the
+// constant  sum_j log sigma_j + (J + 1/2) log 2pi + log mu_scale + log tau_scale + log pi - log 2
+// (the normalisers of the two Normal terms per group, the Normal(mu) and HalfCauchy(tau) priors),
+// computed once on the host; and the reciprocal scales of the priors.
+struct HierData {
+  const float* y;
+  const float* sinv;
+  const double* cmodel;
+  float inv_ms2;  // 1 / mu_scale^2
+  float inv_ts;   // 1 / tau_scale
+};
+
+// Potential and gradient of one model's chain, a warp per chain.  Per group everything is FP32
+// multiplies (no division or logarithm), summed across the warp as float-float pairs; the
+// scalar prior terms use FP32 exp/log1p, and only the final sum is FP64.
+__device__ __forceinline__ void hier_nc_potential_warp(const float* z, float* g, double* __restrict__ pe_out,
+                                                       int J, const float* __restrict__ y,
+                                                       const float* __restrict__ sinv, double cmodel, float inv_ms2,
+                                                       float inv_ts, int lane) {
   const float mu = z[0], lt = z[1];
   const float tau = expf(lt);
-  // per-lane partial sums in FP32 (at most 8 terms for J <= 256), summed across the warp as
-  // float-float pairs
   float lpf = 0.0f, swf = 0.0f, swef = 0.0f;
   for (int j = lane; j < J; j += 32) {
     const float eta = z[2 + j];
-    const float yy = y[j], s = sg[j];
+    const float is = sinv[j];
     const float th = fmaf(tau, eta, mu);
-    const float r = (yy - th) / s;
-    lpf += -0.5f * eta * eta - 0.5f * r * r - logf(s);
-    const float w = r / s;
+    const float r = (y[j] - th) * is;
+    lpf += -0.5f * eta * eta - 0.5f * r * r;
+    const float w = r * is;
     swf += w;
     swef = fmaf(w, eta, swef);
     g[2 + j] = eta - tau * w;
@@ -47,15 +57,14 @@ __device__ __forceinline__ void hier_nc_potential_warp(const float* z, float* g,
     fsw = ff_add(fsw, ff_shfl_xor(fsw, o));
     fswe = ff_add(fswe, ff_shfl_xor(fswe, o));
   }
-  const double lp = ff_value(flp), sw = ff_value(fsw), swe = ff_value(fswe);
   if (lane == 0) {
-    const double dmu = (double)mu, dt = exp((double)lt);
-    const double lp_mu = -0.5 * (dmu / mu_scale) * (dmu / mu_scale) - 0.5 * LOG_2PI - log(mu_scale);
-    const double lp_tau = -LOG_PI - log(tau_scale) - log1p((dt / tau_scale) * (dt / tau_scale)) + LOG_2 + (double)lt;
-    const double total = lp + lp_mu + lp_tau - (double)J * LOG_2PI;  // two N(.) normalisers per group
-    *pe_out = -total;
-    g[0] = (float)(dmu / (mu_scale * mu_scale) - sw);
-    g[1] = (float)(2.0 * dt * dt / (tau_scale * tau_scale + dt * dt) - 1.0 - dt * swe);
+    const float sw = fsw.hi + fsw.lo, swe = fswe.hi + fswe.lo;
+    const float u = tau * inv_ts;
+    const float u2 = u * u;
+    const float lp_prior = -0.5f * mu * mu * inv_ms2 - log1pf(u2) + lt;  // Normal(mu), HalfCauchy(tau) + log-det
+    *pe_out = -(ff_value(flp) + (double)lp_prior - cmodel);
+    g[0] = mu * inv_ms2 - sw;
+    g[1] = 2.0f * u2 / (1.0f + u2) - 1.0f - tau * swe;
   }
 }
 

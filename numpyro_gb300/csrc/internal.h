@@ -45,6 +45,8 @@ struct ModelDev {
   double* part_rr = nullptr;  // horseshoe [row tiles][points]
   void* tc = nullptr;         // tensor-core path state (logreg_tc.cu)
   // horseshoe: X^T [P][pad4(n)] and X [n][pad4(P)] zero-padded, beta^T scratch [pad4(P)][pad4(points)]
+  float* hier_sinv = nullptr;     // hierarchical family: 1/sigma per group
+  double* hier_cmodel = nullptr;  // hierarchical family: per-model constant of the potential
   float* hs_xt = nullptr;
   float* hs_xp = nullptr;
   float* hs_bt = nullptr;
@@ -54,11 +56,12 @@ struct ModelDev {
 // device view of the hierarchical family's data (persistent engine)
 struct HierView {
   const float* y;
-  const float* sg;
+  const float* sinv;
+  const double* cmodel;
   const int32_t* off;
   int cpm;
   int num_models;
-  double mu_scale, tau_scale;
+  float inv_ms2, inv_ts;
 };
 
 // device view of the stochastic-volatility data (persistent engine)

@@ -171,7 +171,7 @@ struct Chain {
     }
     FF tx = ff_from(ax), ty = ff_from(ay);
     g.sum2ff(tx, ty, red);
-    return (ff_value(tx) <= 0.0) || (ff_value(ty) <= 0.0);
+    return ff_le0(tx) || ff_le0(ty);
   }
 
   __device__ void copy(float* dst, const float* src) {
@@ -230,7 +230,7 @@ struct Chain {
     });
     FF tx = ff_from(ax), ty = ff_from(ay);
     g.sum2ff(tx, ty, red);  // also keeps every thread's reads of sv before the next write
-    return (ff_value(tx) <= 0.0) || (ff_value(ty) <= 0.0);
+    return ff_le0(tx) || ff_le0(ty);
   }
   // r = S eps (momentum_generator, hmc.py:92-110) with eps in the scratch row; S row-major
   __device__ void dense_momentum(const float* Smat, float* r_out) {
@@ -1116,7 +1116,7 @@ __global__ void __launch_bounds__(256) persistent_hier_kernel(const AdvParams* _
       if (!(ph == PH_LEAF || ph == PH_HMC || ph == PH_HEUR)) break;
       __syncwarp();  // Q written by other lanes
       hier_nc_potential_warp(P.e.Q + (size_t)c * P.D, P.e.G + (size_t)c * P.D, P.e.PE + c, J, hv.y + j0,
-                             hv.sg + j0, hv.mu_scale, hv.tau_scale, lane);
+                             hv.sinv + j0, hv.cmodel[m], hv.inv_ms2, hv.inv_ts, lane);
       __syncwarp();  // G and PE written by other lanes
       ch.run();
     }

@@ -33,10 +33,10 @@ constexpr double LOG_2 = 0.6931471805599453;
 // ============================================================ hierarchical (non-centred)
 // z = [mu, log tau, theta_base(J)];  warp per point; model m = point / cpm
 __global__ void __launch_bounds__(512) hier_nc_kernel(const float* __restrict__ Q, int npts, int ld,
-                                                      const float* __restrict__ y, const float* __restrict__ sg,
+                                                      const float* __restrict__ y, const float* __restrict__ sinv,
+                                                      const double* __restrict__ cmodel,
                                                       const int32_t* __restrict__ off, int cpm, int num_models,
-                                                      double mu_scale,
-                                                      double tau_scale, double* __restrict__ PE,
+                                                      float inv_ms2, float inv_ts, double* __restrict__ PE,
                                                       float* __restrict__ G, const int32_t* pending) {
   if (pending && *pending == 0) return;
   int c = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);  // a warp per point
@@ -45,8 +45,8 @@ __global__ void __launch_bounds__(512) hier_nc_kernel(const float* __restrict__ 
   int m = c / cpm;
   if (m >= num_models) m = num_models - 1;  // points beyond the configured chains reuse the last model
   int j0 = off[m], J = off[m + 1] - j0;
-  hier_nc_potential_warp(Q + (size_t)c * ld, G + (size_t)c * ld, PE + c, J, y + j0, sg + j0, mu_scale, tau_scale,
-                         lane);
+  hier_nc_potential_warp(Q + (size_t)c * ld, G + (size_t)c * ld, PE + c, J, y + j0, sinv + j0, cmodel[m], inv_ms2,
+                         inv_ts, lane);
 }
 
 // ============================================================ logistic regression (FP32 SIMT)
@@ -498,9 +498,9 @@ cudaError_t launch_potential(ModelDev& m, const float* Q, int npts, double* PE, 
     case 1:
     {
       const int cpb = m.tune.hier_cpb;
-      hier_nc_kernel<<<(npts + cpb - 1) / cpb, 32 * cpb, 0, st>>>(Q, npts, ld, m.y, m.sigma, m.offsets,
-                                                                  m.chains_per_model, m.num_models, m.hyper[0],
-                                                                  m.hyper[1], PE, G, pending);
+      hier_nc_kernel<<<(npts + cpb - 1) / cpb, 32 * cpb, 0, st>>>(
+          Q, npts, ld, m.y, m.hier_sinv, m.hier_cmodel, m.offsets, m.chains_per_model, m.num_models,
+          (float)(1.0 / (m.hyper[0] * m.hyper[0])), (float)(1.0 / m.hyper[1]), PE, G, pending);
     }
       break;
     case 2: {
