@@ -156,6 +156,19 @@ __device__ __forceinline__ FF comp_ff(const Comp32& a) {  // renormalised pair (
   return FF{hi, a.c - (hi - a.s)};
 }
 
+// FP32 digamma by the same recurrence and asymptotic series (A&S 6.3.18)
+__device__ __forceinline__ float digamma_f(float x) {
+  float acc = 0.0f;
+  while (x < 6.0f) {
+    acc -= 1.0f / x;
+    x += 1.0f;
+  }
+  const float r = 1.0f / x, r2 = r * r;
+  const float series =
+      r2 * (1.0f / 12 - r2 * (1.0f / 120 - r2 * (1.0f / 252 - r2 * (1.0f / 240 - r2 * (1.0f / 132)))));
+  return acc + logf(x) - 0.5f * r - series;
+}
+
 // ---------------------------------------------------------------- engine
 enum Phase : int32_t {
   PH_IDLE = 0,

@@ -185,13 +185,17 @@ __global__ void logreg_finish_kernel(const float* __restrict__ Q, int npts, int 
   int c = blockIdx.x * 8 + (threadIdx.x >> 5);
   int lane = threadIdx.x & 31;
   if (c >= npts) return;
-  double inv_var = 1.0 / (prior_scale * prior_scale);
+  const float inv_var_f = (float)(1.0 / (prior_scale * prior_scale));
+  const double inv_var = (double)inv_var_f;
   double lp = 0.0;
   for (int d = lane; d < p; d += 32) {
-    double b = (double)Q[(size_t)c * ld + d];
-    double s = 0.0;
-    for (int r = 0; r < row_groups; ++r) s += (double)part_g[((size_t)r * npts + c) * 64 + d];
-    G[(size_t)c * ld + d] = (float)(s + b * inv_var);
+    const float bf = Q[(size_t)c * ld + d];
+    // the row groups' FP32 gradient partials are summed in FP32 (the gradient is FP32); the
+    // potential's prior and linear terms stay FP64 (lin . b reaches ~1e5 on large data)
+    float s = 0.0f;
+    for (int r = 0; r < row_groups; ++r) s += part_g[((size_t)r * npts + c) * 64 + d];
+    G[(size_t)c * ld + d] = fmaf(bf, inv_var_f, s);
+    const double b = (double)bf;
     lp += 0.5 * b * b * inv_var;
     if (lin) lp += lin[d] * b;
   }

@@ -40,25 +40,29 @@ struct SvSmem {
   float2 warp_tot[2][NT / 32];
 };
 
-// The FP64 scalar factors of the potential, each group on lane 0 of its own warp so they run side
-// by side with the element loop; thread 0 reads them after the reductions' barriers.
+// The scalar factors of the potential, each group on lane 0 of its own warp so they run side by
+// side with the element loop; thread 0 reads them after the reductions' barriers.  The two
+// log-gamma values enter U multiplied by T and grow like x log x, so they stay FP64 (in FP32,
+// T * lgamma(nu/2) rounds to O(1) at large nu and roughens the energy surface).  The digammas
+// enter only through a difference of order 1/nu in the gradient, and the remaining factors need
+// no more than FP32 (GB300 issues FP64 at a small fraction of the FP32 rate).
 template <int NT>
 __device__ __forceinline__ void sv_special_functions(float lnuf, float lsf, double s_rate, double nu_rate, int tid,
                                                      double* special) {
   static_assert(NT >= 256, "needs six warps");
   if ((tid & 31) != 0) return;
-  const double nu = exp((double)lnuf);
+  const float nu = expf(lnuf);
   switch (tid >> 5) {
-    case 0: special[0] = lgamma(0.5 * nu); break;
-    case 1: special[1] = lgamma(0.5 * (nu + 1.0)); break;
-    case 2: special[2] = digamma_d(0.5 * nu); break;
-    case 3: special[3] = digamma_d(0.5 * (nu + 1.0)); break;
-    case 4: special[4] = nu; special[5] = 1.0 / nu; break;
+    case 0: special[0] = lgamma(0.5 * (double)nu); break;
+    case 1: special[1] = lgamma(0.5 * ((double)nu + 1.0)); break;
+    case 2: special[2] = (double)digamma_f(0.5f * nu); break;
+    case 3: special[3] = (double)digamma_f(0.5f * (nu + 1.0f)); break;
+    case 4: special[4] = (double)nu; special[5] = (double)(1.0f / nu); break;
     case 5: {
-      const double s = exp((double)lsf);
-      special[6] = s;
-      special[7] = 1.0 / s;
-      special[8] = log(s_rate) + log(nu_rate);
+      const float s = expf(lsf);
+      special[6] = (double)s;
+      special[7] = (double)(1.0f / s);
+      special[8] = (double)(logf((float)s_rate) + logf((float)nu_rate));
       break;
     }
     default: break;
