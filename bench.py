@@ -306,6 +306,24 @@ def run_reference(args):
     return 0
 
 
+def replica_seed(rank):
+    """Replicas: each rank runs its own chains from its own seed (chains never share a stream
+    address across ranks); nothing is exchanged during sampling."""
+    return 1000 + rank
+
+
+def reduce_over_ranks(dist, total_ms, ess, grad_evals, device="cpu"):
+    """Whole-job figures of a replica run: the slowest rank's time, and the ranks' ESS and
+    gradient evaluations summed (each rank samples independent chains)."""
+    import torch
+
+    t = torch.tensor([total_ms, ess, float(grad_evals)], dtype=torch.float64, device=device)
+    tmax = t.clone()
+    dist.all_reduce(tmax, op=dist.ReduceOp.MAX)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(tmax[0]), float(t[1]), int(t[2])
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -332,7 +350,7 @@ def main():
     model = models.LogisticRegression(X, y)
     C = args.chains
     kernel = NUTS(model, num_chains=C, engine=args.engine, precision=precision)
-    seed = 1000 + rank  # replicas: independent chains per rank
+    seed = replica_seed(rank)
     t0 = time.perf_counter()
     log("init %d chains, precision %s" % (C, precision))
     state = kernel.init(seed, args.num_warmup)
@@ -376,11 +394,7 @@ def main():
     grad_evals = int(torch.cat(nsteps, dim=1).sum().item())
     ess, rhat = min_bulk_ess(z)
     if dist:
-        t = torch.tensor([total_ms, ess, grad_evals], dtype=torch.float64, device="cuda")
-        tmax = t.clone()
-        dist.all_reduce(tmax, op=dist.ReduceOp.MAX)
-        dist.all_reduce(t, op=dist.ReduceOp.SUM)
-        total_ms, ess, grad_evals = float(tmax[0]), float(t[1]), int(t[2])
+        total_ms, ess, grad_evals = reduce_over_ranks(dist, total_ms, ess, grad_evals, device="cuda")
     value = ess / (total_ms / 1e3)
     # ---------------- dominant kernel: the potential, timed alone on the same stream
     log("timed steps done: %.1f ms/step" % (total_ms / max(1, args.steps)))
