@@ -18,12 +18,13 @@
 //                            (three K=64 BF16 products accumulate in FP32 in TMEM, so the
 //                            FP32 coefficients are represented exactly: "bf16x3"),
 //                            GEMM2  G[128 chains x 64 feat] += E . X'_tile  (E = sigmoid(l'))
-//   warps 2..17 epilogue: TMEM lanes are chains, columns rows; 4 warps per lane quadrant split
+//   warps 2..17 epilogue: TMEM lanes are chains, columns rows.  Two groups of 8 warps take
+//               alternate tiles (one H buffer each); in a group 2 warps per lane quadrant split
 //               the 128 rows.  Per logit one ex2 and one tanh; log(1 + e^{-|l'|}) is taken as one
 //               lg2 of the product of 8 rows' factors (2.125 special-function ops per logit).
 //               E goes to shared memory as bf16 in the K-major layout GEMM2 reads.  Each thread
-//               accumulates its chain's log-likelihood over its rows; the four row quarters are
-//               combined once per CTA in FP64.
+//               accumulates its chain's log-likelihood over its rows; the four threads of a
+//               chain are combined once per CTA in FP64.
 // H is double-buffered in TMEM (2 x 128 columns) so GEMM1 of tile t+1 overlaps the
 // epilogue of tile t; G lives in TMEM for the whole launch (64 columns).
 // The design matrix must be exactly representable in bf16 (checked on the host).
@@ -58,6 +59,7 @@ constexpr int OFF_MISC = OFF_S + 2 * S_TILE;
 constexpr int NUM_BARS = 2 * STAGES + 2 + 2 + 2 + 2 + 1;
 constexpr int SMEM_BYTES = OFF_MISC + 256 + BN * 8 + 1024;  // + alignment slack
 constexpr int EPI_WARPS = 16;             // epilogue warps: 4 per TMEM lane quadrant
+constexpr int EPI_GROUP = EPI_WARPS / 2;  // warps that share one tile (one accumulator buffer)
 constexpr int GCOLS = BK * 4 / EPI_WARPS; // gradient columns read back per epilogue warp
 constexpr int NUM_THREADS = 32 * (2 + EPI_WARPS);
 constexpr uint32_t TMEM_COLS = 512;
@@ -77,19 +79,22 @@ enum { B_XFULL = 0, B_XEMPTY = STAGES, B_ACCF = 2 * STAGES, B_ACCE = 2 * STAGES 
 // log-likelihood (their X' rows are zero, so E needs no mask).
 // E is written to erow: this chain's 128-byte row of the swizzled K-major tile, 16-byte chunk
 // chunk0 + g for rows 8g..8g+7, XOR-swizzled with the chain index cx = chain & 7.
+// With release, this warp's last read of the accumulator buffer is signalled on acc_empty_bar.
 template <bool MASK>
 __device__ __forceinline__ void epilogue_tile(uint32_t taddr, uint8_t* erow, int chunk0, int cx, int nvalid,
-                                              float& sabs, float& slg, uint32_t acc_empty_bar, int lane) {
+                                              float& sabs, float& slg, bool release, uint32_t acc_empty_bar,
+                                              int lane) {
   const float NEG_2LOG2E = -2.8853900817779268f;
   uint32_t v[2][16];
   tmem_ld16u(taddr, v[0]);
   tmem_ld16u(taddr + 16, v[1]);
   tmem_wait16(v[0]);
   tmem_wait16(v[1]);
-  // every column of this warp's share has been read: release the accumulator to the MMA warp
-  tc_fence_before();
-  __syncwarp();
-  if (lane == 0) bar_arrive(acc_empty_bar);
+  if (release) {  // every column of this warp's share has been read: release the accumulator
+    tc_fence_before();
+    __syncwarp();
+    if (lane == 0) bar_arrive(acc_empty_bar);
+  }
   float ta = 0.0f, tl = 0.0f;
 #pragma unroll
   for (int g8 = 0; g8 < 4; ++g8) {
@@ -152,8 +157,8 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) logreg_tc_kernel(const __grid_
     }
     for (int i = 0; i < 2; ++i) {
       bar_init(bar(B_ACCF + i), 1);
-      bar_init(bar(B_ACCE + i), EPI_WARPS);
-      bar_init(bar(B_SF + i), EPI_WARPS);
+      bar_init(bar(B_ACCE + i), EPI_GROUP);
+      bar_init(bar(B_SF + i), EPI_GROUP);
       bar_init(bar(B_SE + i), 1);
     }
     bar_init(bar(B_DONE), 1);
@@ -207,89 +212,97 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) logreg_tc_kernel(const __grid_
     }
   } else if (warp == 1) {
     // ------------------------------------------------------------ MMA issuer
-    if (lane == 0) {
-      constexpr uint32_t ID1 = idesc(BN, BM, 0, 0);  // H = B . X'^T: chains x rows, both K-major
-      constexpr uint32_t ID2 = idesc(BN, BK, 0, 1);  // G = E . X': E K-major, X' MN-major
-      const uint32_t xb = smem_u32(smem + OFF_X), bb = smem_u32(smem + OFF_B), sb = smem_u32(smem + OFF_S);
-      bool ok = true;
-      int committed_gemm2 = -1;
-      for (int i = 0; i <= my_tiles && ok; ++i) {
-        if (i < my_tiles) {
-          int s = i % STAGES, b = i & 1;
-          ok = bar_wait(bar(B_XFULL + s), (i / STAGES) & 1, abort_flag, P.err);
-          if (ok && i >= 2) ok = bar_wait(bar(B_ACCE + b), ((i >> 1) - 1) & 1, abort_flag, P.err);
-          if (!ok) break;
-          tc_fence_after();
-          const uint32_t d = tmem + (uint32_t)(b * BN);
-          int first = 1;
+    // The whole warp runs this loop and one elected lane issues each MMA and commit: from a
+    // converged warp the descriptor arithmetic stays warp-uniform.  (Run by lane 0 alone,
+    // each tcgen05.mma took ~70-90 cycles to issue and this loop, not the tensor pipe or the
+    // epilogue, set the tile rate.)  Descriptors are built once and moved by constant offsets.
+    constexpr uint32_t ID1 = idesc(BN, BM, 0, 0);  // H = B . X'^T: chains x rows, both K-major
+    constexpr uint32_t ID2 = idesc(BN, BK, 0, 1);  // G = E . X': E K-major, X' MN-major
+    const uint32_t xb = smem_u32(smem + OFF_X), bb = smem_u32(smem + OFF_B), sb = smem_u32(smem + OFF_S);
+    const uint64_t dcoef = sdesc(bb, 16, 1024);  // GEMM1 A: the coefficient splits, the same every tile
+    const uint64_t dx1 = sdesc(xb, 16, 1024);    // GEMM1 B: X' tile, K-major, stage 0
+    const uint64_t dx2 = sdesc(xb, 1024, 1024);  // GEMM2 B: X' tile, MN-major, stage 0
+    const uint64_t de = sdesc(sb, 16, 1024);     // GEMM2 A: E tile, K-major, buffer 0
+    bool ok = true;
+    for (int i = 0; i <= my_tiles && ok; ++i) {
+      if (i < my_tiles) {
+        int s = i % STAGES, b = i & 1;
+        ok = bar_wait_warp(bar(B_XFULL + s), (i / STAGES) & 1, abort_flag, P.err);
+        if (ok && i >= 2) ok = bar_wait_warp(bar(B_ACCE + b), ((i >> 1) - 1) & 1, abort_flag, P.err);
+        if (!ok) break;
+        tc_fence_after();
+        const uint32_t d = tmem + (uint32_t)(b * BN);
+        const uint64_t xs = sdesc_at(dx1, (uint32_t)(s * X_TILE));
 #pragma unroll
-          for (int k = 0; k < NSPLIT; ++k) {
+        for (int k = 0; k < NSPLIT; ++k) {
 #pragma unroll
-            for (int kk = 0; kk < BK / 16; ++kk) {
-              uint64_t a = sdesc(bb + k * B_TILE + kk * 32, 16, 1024);
-              uint64_t bd = sdesc(xb + s * X_TILE + kk * 32, 16, 1024);
-              mma_bf16(d, a, bd, ID1, first ? 0u : 1u);
-              first = 0;
-            }
-          }
-          mma_commit(bar(B_ACCF + b));
+          for (int kk = 0; kk < BK / 16; ++kk)
+            mma_bf16_warp(d, sdesc_at(dcoef, k * B_TILE + kk * 32), sdesc_at(xs, kk * 32), ID1,
+                          (k | kk) ? 1u : 0u);
         }
-        if (i >= 1) {
-          int j = i - 1, s = j % STAGES, b = j & 1;
-          ok = bar_wait(bar(B_SF + b), (j >> 1) & 1, abort_flag, P.err);
-          if (!ok) break;
-          tc_fence_after();
+        mma_commit_warp(bar(B_ACCF + b));
+      }
+      if (i >= 1) {
+        int j = i - 1, s = j % STAGES, b = j & 1;
+        ok = bar_wait_warp(bar(B_SF + b), (j >> 1) & 1, abort_flag, P.err);
+        if (!ok) break;
+        tc_fence_after();
+        const uint64_t eb = sdesc_at(de, (uint32_t)(b * S_TILE)), xs = sdesc_at(dx2, (uint32_t)(s * X_TILE));
 #pragma unroll
-          for (int kk = 0; kk < BM / 16; ++kk) {
-            // A = E[b]: K-major [128 chains][128 rows] as two 64-row swizzled halves of 16 KB
-            uint64_t a = sdesc(sb + b * S_TILE + (kk >> 2) * (BN * 64 * 2) + (kk & 3) * 32, 16, 1024);
-            // B = X tile: MN-major (features contiguous), 8-row groups 1024 B apart (SBO)
-            uint64_t bd = sdesc(xb + s * X_TILE + kk * 2048, 1024, 1024);
-            mma_bf16(tmem + ACC2_COL, a, bd, ID2, (j > 0 || kk > 0) ? 1u : 0u);
-          }
-          mma_commit(bar(B_SE + b));
-          mma_commit(bar(B_XEMPTY + s));
-          committed_gemm2 = j;
+        for (int kk = 0; kk < BM / 16; ++kk) {
+          // A = E[b]: K-major [128 chains][128 rows] as two 64-row swizzled halves of 16 KB
+          // B = X tile: MN-major (features contiguous), 8-row groups 1024 B apart (SBO)
+          mma_bf16_warp(tmem + ACC2_COL, sdesc_at(eb, (kk >> 2) * (BN * 64 * 2) + (kk & 3) * 32),
+                        sdesc_at(xs, kk * 2048), ID2, (j > 0 || kk > 0) ? 1u : 0u);
         }
+        mma_commit_warp(bar(B_SE + b));
+        mma_commit_warp(bar(B_XEMPTY + s));
       }
-      mma_commit(bar(B_DONE));
-      (void)committed_gemm2;
-      // wait for every MMA issued by this thread before TMEM can be released
-      for (uint32_t k = 0; k < WAIT_LIMIT && !bar_try(bar(B_DONE), 0); ++k) {
-      }
+    }
+    __syncwarp();
+    mma_commit_warp(bar(B_DONE));
+    // wait for every MMA issued by this warp before TMEM can be released
+    for (uint32_t k = 0; k < WAIT_LIMIT && !bar_try(bar(B_DONE), 0); ++k) {
     }
   } else {
     // ------------------------------------------------------------ epilogue (warps 2..17)
+    // Two groups of 8 warps take alternate tiles, each group one accumulator buffer, so that
+    // the groups' TMEM loads and special-function bursts interleave instead of coinciding.
+    // In a group, 2 warps per TMEM lane quadrant each take a 64-row half of the tile, as two
+    // 32-row parts.
     const int ew = warp - 2;
     const int q = warp & 3;          // TMEM lane quadrant this warp may access: chains 32q..32q+31
-    const int rq = ew >> 2;          // row quarter of each tile: rows 32 rq .. 32 rq + 31
+    const int grp = ew / EPI_GROUP;  // tiles i with i % 2 == grp, accumulator buffer grp
+    const int rh = (ew >> 2) & 1;    // row half of each tile: rows 64 rh .. 64 rh + 63
     const int c = q * 32 + lane;     // this thread's chain within the CTA
-    const uint32_t tl = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(rq * 32);
-    // this chain's row of the E tile (K-major, rows 64 (rq / 2) .. of the tile)
-    uint8_t* erow0 = smem + OFF_S + (rq >> 1) * (BN * 64 * 2) + (c >> 3) * 1024 + (c & 7) * 128;
+    const uint32_t tl = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(grp * BM + rh * 64);
+    // this chain's row of the group's E tile (K-major, the 64-row swizzled half rh)
+    uint8_t* erow = smem + OFF_S + grp * S_TILE + rh * (BN * 64 * 2) + (c >> 3) * 1024 + (c & 7) * 128;
     Comp32 ll{0.0f, 0.0f};  // log-likelihood of this chain over this thread's rows, all tiles
     bool ok = true;
-    for (int i = 0; i < my_tiles && ok; ++i) {
-      const int b = i & 1;
-      const int64_t row0 = ((int64_t)rg + (int64_t)i * P.row_groups) * BM;
-      ok = bar_wait(bar(B_ACCF + b), (i >> 1) & 1, abort_flag, P.err);
-      if (ok && i >= 2) ok = bar_wait(bar(B_SE + b), ((i >> 1) - 1) & 1, abort_flag, P.err);
+    for (int i = grp; i < my_tiles && ok; i += 2) {
+      const int64_t row0 = ((int64_t)rg + (int64_t)i * P.row_groups) * BM + rh * 64;
+      ok = bar_wait(bar(B_ACCF + grp), (i >> 1) & 1, abort_flag, P.err);
+      if (ok && i >= 2) ok = bar_wait(bar(B_SE + grp), ((i >> 1) - 1) & 1, abort_flag, P.err);
       if (!ok) break;
       tc_fence_after();
-      float sabs = 0.0f, slg = 0.0f;
-      const int64_t nleft = P.n - (row0 + rq * 32);
-      if (nleft >= 32)
-        epilogue_tile<false>(tl + (uint32_t)(b * BM), erow0 + b * S_TILE, (rq & 1) * 4, c & 7, 32, sabs, slg,
-                             bar(B_ACCE + b), lane);
-      else
-        epilogue_tile<true>(tl + (uint32_t)(b * BM), erow0 + b * S_TILE, (rq & 1) * 4, c & 7,
-                            nleft > 0 ? (int)nleft : 0, sabs, slg, bar(B_ACCE + b), lane);
-      ll.add(fmaf(0.6931471805599453f, slg, sabs));
+#pragma unroll
+      for (int part = 0; part < 2; ++part) {
+        float sabs = 0.0f, slg = 0.0f;
+        const int64_t nleft = P.n - (row0 + part * 32);
+        if (nleft >= 32)
+          epilogue_tile<false>(tl + (uint32_t)(part * 32), erow, part * 4, c & 7, 32, sabs, slg, part == 1,
+                               bar(B_ACCE + grp), lane);
+        else
+          epilogue_tile<true>(tl + (uint32_t)(part * 32), erow, part * 4, c & 7, nleft > 0 ? (int)nleft : 0,
+                              sabs, slg, part == 1, bar(B_ACCE + grp), lane);
+        ll.add(fmaf(0.6931471805599453f, slg, sabs));
+      }
       fence_proxy_async();
       __syncwarp();
-      if (lane == 0) bar_arrive(bar(B_SF + b));
+      if (lane == 0) bar_arrive(bar(B_SF + grp));
     }
-    // per-chain sums over the CTA's rows: the four row quarters meet in shared memory (FP64)
+    // per-chain sums over the CTA's rows: the chain's four threads meet in shared memory (FP64)
     if (ok) atomicAdd(&ll_smem[c], comp_total(ll));
     // gradient partials: G (lanes = chains, 64 feature columns)
     if (ok) ok = bar_wait(bar(B_DONE), 0, abort_flag, P.err);
@@ -299,7 +312,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) logreg_tc_kernel(const __grid_
 #pragma unroll
       for (int j = 0; j < GCOLS / 16; ++j) {
         float v[16];
-        const int colb = rq * GCOLS + j * 16;
+        const int colb = (ew >> 2) * GCOLS + j * 16;  // 4 warps per lane quadrant split the 64 columns
         tmem_ld16(tmem + ((uint32_t)(q * 32) << 16) + ACC2_COL + (uint32_t)colb, v);
         tmem_wait_ld();
         if (gc < P.npts) {

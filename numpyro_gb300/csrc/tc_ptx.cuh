@@ -45,6 +45,19 @@ __device__ __forceinline__ bool bar_wait(uint32_t a, uint32_t parity, volatile i
   atomicExch(err, 4);
   return false;
 }
+// bounded wait by a whole converged warp: every lane leaves on the same poll
+__device__ __forceinline__ bool bar_wait_warp(uint32_t a, uint32_t parity, volatile int* abort_flag, int* err) {
+  for (uint32_t i = 0; i < WAIT_LIMIT; ++i) {
+    if (__all_sync(0xffffffffu, bar_try(a, parity))) return true;
+    if (__any_sync(0xffffffffu, *abort_flag != 0)) return false;
+  }
+  if ((threadIdx.x & 31) == 0) {
+    *abort_flag = 1;
+    atomicExch(err, 4);
+  }
+  __syncwarp();
+  return false;
+}
 __device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
@@ -63,6 +76,13 @@ __device__ __forceinline__ uint64_t sdesc(uint32_t addr, uint32_t lbo, uint32_t 
   return (uint64_t)((addr >> 4) & 0x3FFFu) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
          ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46) | (2ull << 61);
 }
+// The descriptor of a tile `bytes` (a multiple of 16) further on: the start-address field is
+// the low 14 bits of the low word, and shared-memory addresses stay below 256 KB, so the add
+// never carries out of the field.  One 32-bit add instead of rebuilding the descriptor.
+__device__ __forceinline__ uint64_t sdesc_at(uint64_t d, uint32_t bytes) {
+  const uint32_t lo = (uint32_t)d + (bytes >> 4), hi = (uint32_t)(d >> 32);
+  return ((uint64_t)hi << 32) | lo;
+}
 // instruction descriptor, kind::f16: D=f32 (bit 4), A=B=bf16 (bits 7, 10), A/B major at 15/16,
 // N>>3 at [17,23), M>>4 at [24,29)
 __host__ __device__ constexpr uint32_t idesc(int M, int N, int a_mn_major, int b_mn_major) {
@@ -74,6 +94,22 @@ __device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t a, uint64_t b
       "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
       "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem_d),
       "l"(a), "l"(b), "r"(id), "r"(acc)
+      : "memory");
+}
+// The same, executed by a whole converged warp: one elected lane issues the MMA.  Issuing from
+// a converged warp keeps the descriptor arithmetic warp-uniform; from inside `if (lane == 0)`
+// every MMA cost ~70-90 cycles of issue latency.
+__device__ __forceinline__ void mma_bf16_warp(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t id, uint32_t acc) {
+  asm volatile(
+      "{\n\t.reg .pred p, e;\n\telect.sync _|e, 0xffffffff;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+      "@e tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem_d),
+      "l"(a), "l"(b), "r"(id), "r"(acc)
+      : "memory");
+}
+__device__ __forceinline__ void mma_commit_warp(uint32_t bar) {
+  asm volatile(
+      "{\n\t.reg .pred e;\n\telect.sync _|e, 0xffffffff;\n\t"
+      "@e tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n\t}" ::"r"(bar)
       : "memory");
 }
 __device__ __forceinline__ void mma_commit(uint32_t bar) {
