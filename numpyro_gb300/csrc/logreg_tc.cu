@@ -13,20 +13,24 @@
 // is added per chain from a vector computed once.
 //
 // One CTA owns 128 chains and a strided set of 128-row tiles of X':
-//   warp 0      TMA producer: X' tile [128 rows x 64 feat] bf16, 128B swizzle, 4-stage ring
+//   warp 0      TMA producer: X' tile [128 rows x 64 feat] bf16, 128B swizzle, 8-stage ring,
+//               with an L2 prefetch running 8 tiles ahead
 //   warp 1      MMA issuer:  GEMM1  H[128 chains x 128 rows] = (b_hi + b_mid + b_lo)/2 . X'_tile^T
 //                            (three K=64 BF16 products accumulate in FP32 in TMEM, so the
 //                            FP32 coefficients are represented exactly: "bf16x3"),
-//                            GEMM2  G[128 chains x 64 feat] += E . X'_tile  (E = sigmoid(l'))
+//                            GEMM2  G[128 chains x 64 feat] += E . X'_tile  (E = sigmoid(l'),
+//                            the A operand read from TMEM)
 //   warps 2..17 epilogue: TMEM lanes are chains, columns rows.  Two groups of 8 warps take
-//               alternate tiles (one H buffer each); in a group 2 warps per lane quadrant split
-//               the 128 rows.  Per logit one ex2 and one tanh; log(1 + e^{-|l'|}) is taken as one
-//               lg2 of the product of 8 rows' factors (2.125 special-function ops per logit).
-//               E goes to shared memory as bf16 in the K-major layout GEMM2 reads.  Each thread
-//               accumulates its chain's log-likelihood over its rows; the four threads of a
-//               chain are combined once per CTA in FP64.
-// H is double-buffered in TMEM (2 x 128 columns) so GEMM1 of tile t+1 overlaps the
-// epilogue of tile t; G lives in TMEM for the whole launch (64 columns).
+//               alternate tiles; in a group 2 warps per lane quadrant split the 128 rows.  Per
+//               logit one ex2 and one tanh; log(1 + e^{-|l'|}) is taken as one lg2 of the product
+//               of 8 rows' factors (2.125 special-function ops per logit).  E goes back to TMEM
+//               as bf16 pairs, into columns of the same H buffer the warp has already read.
+//               Each thread accumulates its chain's log-likelihood over its rows; the four
+//               threads of a chain are combined once per CTA in FP64.
+// Three H buffers in TMEM (3 x 128 columns) keep three tiles in flight, and GEMM2 of tile t is
+// issued after GEMM1 of tile t + 2; G lives in TMEM for the whole launch (64 columns).  Keeping
+// E in TMEM leaves shared memory to the X' and coefficient operands: with E in shared memory
+// as well (its stores plus GEMM2 reading it), the tensor pipe waited on shared-memory bandwidth.
 // The design matrix must be exactly representable in bf16 (checked on the host).
 // Every mbarrier wait is bounded; on a timeout the CTA records an error, drains its
 // in-flight copies and MMAs (bounded), frees TMEM and returns.
@@ -48,58 +52,57 @@ constexpr int BM = 128;  // rows per tile
 constexpr int BN = 128;  // chains per CTA
 constexpr int BK = 64;   // padded features: one 128-byte swizzle row of bf16
 constexpr int NSPLIT = 3;
-constexpr int STAGES = 4;
+constexpr int STAGES = 8;  // X' tiles stay resident until GEMM2, LAG tiles after GEMM1
 constexpr int X_TILE = BM * BK * 2;  // 16 KB
 constexpr int B_TILE = BN * BK * 2;  // 16 KB
-constexpr int S_TILE = BM * BN * 2;  // 32 KB
+constexpr int NBUF = 3;              // H buffers in TMEM (each also holds its tile's E): tiles in flight
+constexpr int PREFETCH = 8;          // X' tiles an L2 prefetch runs ahead of the loads
+constexpr int LAG = 2;               // GEMM2 of tile i - LAG is issued after GEMM1 of tile i
 constexpr int OFF_X = 0;
 constexpr int OFF_B = OFF_X + STAGES * X_TILE;
-constexpr int OFF_S = OFF_B + NSPLIT * B_TILE;
-constexpr int OFF_MISC = OFF_S + 2 * S_TILE;
-constexpr int NUM_BARS = 2 * STAGES + 2 + 2 + 2 + 2 + 1;
+constexpr int OFF_MISC = OFF_B + NSPLIT * B_TILE;
+constexpr int NUM_BARS = 2 * STAGES + 3 * NBUF + 1;
 constexpr int SMEM_BYTES = OFF_MISC + 256 + BN * 8 + 1024;  // + alignment slack
 constexpr int EPI_WARPS = 16;             // epilogue warps: 4 per TMEM lane quadrant
 constexpr int EPI_GROUP = EPI_WARPS / 2;  // warps that share one tile (one accumulator buffer)
 constexpr int GCOLS = BK * 4 / EPI_WARPS; // gradient columns read back per epilogue warp
 constexpr int NUM_THREADS = 32 * (2 + EPI_WARPS);
 constexpr uint32_t TMEM_COLS = 512;
-constexpr uint32_t ACC2_COL = 256;
+constexpr uint32_t ACC2_COL = NBUF * BM;  // G after the H buffers
 
-enum { B_XFULL = 0, B_XEMPTY = STAGES, B_ACCF = 2 * STAGES, B_ACCE = 2 * STAGES + 2, B_SF = 2 * STAGES + 4,
-       B_SE = 2 * STAGES + 6, B_DONE = 2 * STAGES + 8 };
+// ACCF: GEMM1 wrote H; SF: the epilogue wrote E (into the same buffer); SE: GEMM2 has read E, the
+// buffer is free for GEMM1 again
+enum { B_XFULL = 0, B_XEMPTY = STAGES, B_ACCF = 2 * STAGES, B_SF = B_ACCF + NBUF, B_SE = B_SF + NBUF,
+       B_DONE = B_SE + NBUF };
+static_assert(LAG < NBUF, "GEMM1 of tile i reuses the buffer GEMM2 of tile i - NBUF reads");
+static_assert(ACC2_COL + BK <= TMEM_COLS, "TMEM holds the H buffers and G");
+static_assert(SMEM_BYTES <= 232448, "shared memory per CTA");
+static_assert(NUM_BARS * 8 + 8 <= 256, "barriers, TMEM address and abort flag fit their slot");
 
-// One tile of the epilogue for one warp: its lane's chain x 32 rows (TMEM columns at taddr).
+// One part of the epilogue for one warp: its lane's chain x 32 rows (TMEM columns at th).
 // TMEM holds h = l'/2 (the coefficients enter GEMM1 halved, an exact scaling).  Per row:
-//   E = sigmoid(l') = tanh(h)/2 + 1/2                      -> bf16, K-major tile for GEMM2
-//       (forming it by Newton's method on the FMA pipe for half the rows measured slower:
-//       with 2.125 special-function ops per logit the epilogue is issue-bound)
+//   E = sigmoid(l') = tanh(h)/2 + 1/2                      -> bf16, GEMM2's A operand in TMEM
+//       (forming it from e^{-2|h|} on the FMA pipe, with one reciprocal per 8 rows or by
+//       Newton's method, measured slower)
 //   softplus(l') - l'/2 = |h| + log(1 + e^{-2|h|})          -> |h| summed, the logs taken as
 //                                                            one log2 per product of 8 rows
 // With MASK, rows r >= nvalid lie past the end of the data: they are left out of the
 // log-likelihood (their X' rows are zero, so E needs no mask).
-// E is written to erow: this chain's 128-byte row of the swizzled K-major tile, 16-byte chunk
-// chunk0 + g for rows 8g..8g+7, XOR-swizzled with the chain index cx = chain & 7.
-// With release, this warp's last read of the accumulator buffer is signalled on acc_empty_bar.
+// E goes to the 16 TMEM columns at te, two rows per column (the even row in the low half):
+// columns this warp has already read, so H and E share the buffer.
 template <bool MASK>
-__device__ __forceinline__ void epilogue_tile(uint32_t taddr, uint8_t* erow, int chunk0, int cx, int nvalid,
-                                              float& sabs, float& slg, bool release, uint32_t acc_empty_bar,
-                                              int lane) {
+__device__ __forceinline__ void epilogue_part(uint32_t th, uint32_t te, int nvalid, float& sabs, float& slg) {
   const float NEG_2LOG2E = -2.8853900817779268f;
   uint32_t v[2][16];
-  tmem_ld16u(taddr, v[0]);
-  tmem_ld16u(taddr + 16, v[1]);
+  tmem_ld16u(th, v[0]);
+  tmem_ld16u(th + 16, v[1]);
   tmem_wait16(v[0]);
   tmem_wait16(v[1]);
-  if (release) {  // every column of this warp's share has been read: release the accumulator
-    tc_fence_before();
-    __syncwarp();
-    if (lane == 0) bar_arrive(acc_empty_bar);
-  }
   float ta = 0.0f, tl = 0.0f;
+  uint32_t pk[16];
 #pragma unroll
   for (int g8 = 0; g8 < 4; ++g8) {
     float prod = 1.0f;
-    uint32_t pk[4];
 #pragma unroll
     for (int e = 0; e < 8; e += 2) {
       float ev[2];
@@ -114,11 +117,11 @@ __device__ __forceinline__ void epilogue_tile(uint32_t taddr, uint8_t* erow, int
         }
         ev[hh] = fmaf(0.5f, tanh_approx(h), 0.5f);
       }
-      pk[e >> 1] = pack_bf16(ev[0], ev[1]);
+      pk[4 * g8 + (e >> 1)] = pack_bf16(ev[0], ev[1]);
     }
     tl += lg2_approx(prod);
-    *reinterpret_cast<uint4*>(erow + (((chunk0 + g8) ^ cx) << 4)) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
   }
+  tmem_st16(te, pk);
   sabs += ta;
   slg += tl;
 }
@@ -155,9 +158,8 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) logreg_tc_kernel(const __grid_
       bar_init(bar(B_XFULL + i), 1);
       bar_init(bar(B_XEMPTY + i), 1);
     }
-    for (int i = 0; i < 2; ++i) {
+    for (int i = 0; i < NBUF; ++i) {
       bar_init(bar(B_ACCF + i), 1);
-      bar_init(bar(B_ACCE + i), EPI_GROUP);
       bar_init(bar(B_SF + i), EPI_GROUP);
       bar_init(bar(B_SE + i), 1);
     }
@@ -198,6 +200,10 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) logreg_tc_kernel(const __grid_
         int s = i % STAGES;
         if (i >= STAGES && !bar_wait(bar(B_XEMPTY + s), ((i / STAGES) - 1) & 1, abort_flag, P.err)) break;
         int64_t row0 = ((int64_t)rg + (int64_t)i * P.row_groups) * BM;
+        // X' tiles are held until GEMM2, so a stage frees only a little ahead of its next use:
+        // pull the tile PREFETCH loads ahead into L2 now, so the load later hits L2
+        if (i + PREFETCH < my_tiles)
+          tma_prefetch_2d(&tmap_x, 0, (int)(row0 + (int64_t)PREFETCH * P.row_groups * BM));
         bar_expect_tx(bar(B_XFULL + s), X_TILE);
         tma_load_2d(smem_u32(smem + OFF_X + s * X_TILE), &tmap_x, 0, (int)row0, bar(B_XFULL + s));
         issued = i + 1;
@@ -217,22 +223,29 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) logreg_tc_kernel(const __grid_
     // each tcgen05.mma took ~70-90 cycles to issue and this loop, not the tensor pipe or the
     // epilogue, set the tile rate.)  Descriptors are built once and moved by constant offsets.
     constexpr uint32_t ID1 = idesc(BN, BM, 0, 0);  // H = B . X'^T: chains x rows, both K-major
-    constexpr uint32_t ID2 = idesc(BN, BK, 0, 1);  // G = E . X': E K-major, X' MN-major
-    const uint32_t xb = smem_u32(smem + OFF_X), bb = smem_u32(smem + OFF_B), sb = smem_u32(smem + OFF_S);
+    constexpr uint32_t ID2 = idesc(BN, BK, 0, 1);  // G = E . X': E K-major in TMEM, X' MN-major
+    const uint32_t xb = smem_u32(smem + OFF_X), bb = smem_u32(smem + OFF_B);
     const uint64_t dcoef = sdesc(bb, 16, 1024);  // GEMM1 A: the coefficient splits, the same every tile
     const uint64_t dx1 = sdesc(xb, 16, 1024);    // GEMM1 B: X' tile, K-major, stage 0
     const uint64_t dx2 = sdesc(xb, 1024, 1024);  // GEMM2 B: X' tile, MN-major, stage 0
-    const uint64_t de = sdesc(sb, 16, 1024);     // GEMM2 A: E tile, K-major, buffer 0
     bool ok = true;
-    for (int i = 0; i <= my_tiles && ok; ++i) {
+    // Tile i uses H buffer i % NBUF; the k-th use of a buffer completes its barriers' phase k.
+    // GEMM2 takes its A operand (E) from TMEM, where the epilogue wrote it into the tile's own H
+    // buffer, so shared memory carries only the X' and coefficient operands (as operands, both
+    // GEMMs read shared memory at close to its bandwidth).  GEMM1(i) first waits for X' tile i
+    // and for GEMM2 of tile i - NBUF to have read the buffer; GEMM2(i - LAG) then waits for its
+    // E.  The chain epilogue -> GEMM2 -> GEMM1 -> epilogue so spans LAG + 1 tiles.  tcgen05.mma
+    // issue is paced by execution (a shallow queue); stages, buffers and parities are counters.
+    int si = 0, pi = 0, bi = 0, qi = 0;  // tile i: X' stage, its fill parity; H buffer, its use parity
+    int sj = 0, bj = 0, qj = 0;          // tile j = i - LAG: X' stage; buffer, its use parity
+    for (int i = 0; i < my_tiles + LAG; ++i) {
       if (i < my_tiles) {
-        int s = i % STAGES, b = i & 1;
-        ok = bar_wait_warp(bar(B_XFULL + s), (i / STAGES) & 1, abort_flag, P.err);
-        if (ok && i >= 2) ok = bar_wait_warp(bar(B_ACCE + b), ((i >> 1) - 1) & 1, abort_flag, P.err);
+        ok = bar_wait3_warp(bar(B_XFULL + si), pi, true, bar(B_SE + bi), qi ^ 1, i >= NBUF, 0u, 0u, false,
+                            abort_flag, P.err);
         if (!ok) break;
         tc_fence_after();
-        const uint32_t d = tmem + (uint32_t)(b * BN);
-        const uint64_t xs = sdesc_at(dx1, (uint32_t)(s * X_TILE));
+        const uint32_t d = tmem + (uint32_t)(bi * BM);
+        const uint64_t xs = sdesc_at(dx1, (uint32_t)(si * X_TILE));
 #pragma unroll
         for (int k = 0; k < NSPLIT; ++k) {
 #pragma unroll
@@ -240,23 +253,28 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) logreg_tc_kernel(const __grid_
             mma_bf16_warp(d, sdesc_at(dcoef, k * B_TILE + kk * 32), sdesc_at(xs, kk * 32), ID1,
                           (k | kk) ? 1u : 0u);
         }
-        mma_commit_warp(bar(B_ACCF + b));
+        mma_commit_warp(bar(B_ACCF + bi));
+        if (++si == STAGES) si = 0, pi ^= 1;
+        if (++bi == NBUF) bi = 0, qi ^= 1;
       }
-      if (i >= 1) {
-        int j = i - 1, s = j % STAGES, b = j & 1;
-        ok = bar_wait_warp(bar(B_SF + b), (j >> 1) & 1, abort_flag, P.err);
+      if (i >= LAG) {
+        const int j = i - LAG;
+        ok = bar_wait_warp(bar(B_SF + bj), qj, abort_flag, P.err);  // E of tile j is in TMEM
         if (!ok) break;
         tc_fence_after();
-        const uint64_t eb = sdesc_at(de, (uint32_t)(b * S_TILE)), xs = sdesc_at(dx2, (uint32_t)(s * X_TILE));
+        const uint32_t ea = tmem + (uint32_t)(bj * BM);
+        const uint64_t xs = sdesc_at(dx2, (uint32_t)(sj * X_TILE));
 #pragma unroll
         for (int kk = 0; kk < BM / 16; ++kk) {
-          // A = E[b]: K-major [128 chains][128 rows] as two 64-row swizzled halves of 16 KB
-          // B = X tile: MN-major (features contiguous), 8-row groups 1024 B apart (SBO)
-          mma_bf16_warp(tmem + ACC2_COL, sdesc_at(eb, (kk >> 2) * (BN * 64 * 2) + (kk & 3) * 32),
-                        sdesc_at(xs, kk * 2048), ID2, (j > 0 || kk > 0) ? 1u : 0u);
+          // A = E rows 16kk..16kk+15: 8 TMEM columns in row half kk / 4 (rows 64 h + r at column
+          // 64 h + r / 2); B = X' tile, MN-major (features contiguous), 8-row groups 1024 B apart
+          mma_bf16_tmem_a_warp(tmem + ACC2_COL, ea + (uint32_t)((kk >> 2) * 64 + (kk & 3) * 8),
+                               sdesc_at(xs, kk * 2048), ID2, (j > 0 || kk > 0) ? 1u : 0u);
         }
-        mma_commit_warp(bar(B_SE + b));
-        mma_commit_warp(bar(B_XEMPTY + s));
+        mma_commit_warp(bar(B_SE + bj));
+        mma_commit_warp(bar(B_XEMPTY + sj));
+        if (++sj == STAGES) sj = 0;
+        if (++bj == NBUF) bj = 0, qj ^= 1;
       }
     }
     __syncwarp();
@@ -266,41 +284,41 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) logreg_tc_kernel(const __grid_
     }
   } else {
     // ------------------------------------------------------------ epilogue (warps 2..17)
-    // Two groups of 8 warps take alternate tiles, each group one accumulator buffer, so that
-    // the groups' TMEM loads and special-function bursts interleave instead of coinciding.
+    // Two groups of 8 warps take alternate tiles, so that the groups' TMEM loads and
+    // special-function bursts interleave instead of coinciding.
     // In a group, 2 warps per TMEM lane quadrant each take a 64-row half of the tile, as two
     // 32-row parts.
     const int ew = warp - 2;
     const int q = warp & 3;          // TMEM lane quadrant this warp may access: chains 32q..32q+31
-    const int grp = ew / EPI_GROUP;  // tiles i with i % 2 == grp, accumulator buffer grp
+    const int grp = ew / EPI_GROUP;  // tiles i with i % 2 == grp
     const int rh = (ew >> 2) & 1;    // row half of each tile: rows 64 rh .. 64 rh + 63
     const int c = q * 32 + lane;     // this thread's chain within the CTA
-    const uint32_t tl = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(grp * BM + rh * 64);
-    // this chain's row of the group's E tile (K-major, the 64-row swizzled half rh)
-    uint8_t* erow = smem + OFF_S + grp * S_TILE + rh * (BN * 64 * 2) + (c >> 3) * 1024 + (c & 7) * 128;
+    const uint32_t tl = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(rh * 64);
     Comp32 ll{0.0f, 0.0f};  // log-likelihood of this chain over this thread's rows, all tiles
     bool ok = true;
     for (int i = grp; i < my_tiles && ok; i += 2) {
       const int64_t row0 = ((int64_t)rg + (int64_t)i * P.row_groups) * BM + rh * 64;
-      ok = bar_wait(bar(B_ACCF + grp), (i >> 1) & 1, abort_flag, P.err);
-      if (ok && i >= 2) ok = bar_wait(bar(B_SE + grp), ((i >> 1) - 1) & 1, abort_flag, P.err);
+      const int b = i % NBUF;
+      ok = bar_wait(bar(B_ACCF + b), (i / NBUF) & 1, abort_flag, P.err);
       if (!ok) break;
       tc_fence_after();
 #pragma unroll
       for (int part = 0; part < 2; ++part) {
         float sabs = 0.0f, slg = 0.0f;
         const int64_t nleft = P.n - (row0 + part * 32);
+        // H of rows 64 rh + 32 part .. +31 is read from columns 64 rh + 32 part; their E goes to
+        // columns 64 rh + 16 part .. +15, which part 0 has already read
+        const uint32_t th = tl + (uint32_t)(b * BM + part * 32), te = tl + (uint32_t)(b * BM + part * 16);
         if (nleft >= 32)
-          epilogue_tile<false>(tl + (uint32_t)(part * 32), erow, part * 4, c & 7, 32, sabs, slg, part == 1,
-                               bar(B_ACCE + grp), lane);
+          epilogue_part<false>(th, te, 32, sabs, slg);
         else
-          epilogue_tile<true>(tl + (uint32_t)(part * 32), erow, part * 4, c & 7, nleft > 0 ? (int)nleft : 0,
-                              sabs, slg, part == 1, bar(B_ACCE + grp), lane);
+          epilogue_part<true>(th, te, nleft > 0 ? (int)nleft : 0, sabs, slg);
         ll.add(fmaf(0.6931471805599453f, slg, sabs));
       }
-      fence_proxy_async();
+      tmem_wait_st();  // E is in TMEM before GEMM2 may read it
+      tc_fence_before();
       __syncwarp();
-      if (lane == 0) bar_arrive(bar(B_SF + grp));
+      if (lane == 0) bar_arrive(bar(B_SF + b));
     }
     // per-chain sums over the CTA's rows: the chain's four threads meet in shared memory (FP64)
     if (ok) atomicAdd(&ll_smem[c], comp_total(ll));

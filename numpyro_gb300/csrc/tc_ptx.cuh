@@ -45,6 +45,40 @@ __device__ __forceinline__ bool bar_wait(uint32_t a, uint32_t parity, volatile i
   atomicExch(err, 4);
   return false;
 }
+// non-blocking probe of a phase (mbarrier.test_wait never suspends the thread)
+__device__ __forceinline__ bool bar_test(uint32_t a, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tmbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(a), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// bounded wait of a whole converged warp for up to three phases at once (each only when its
+// use flag is set): the probes are issued back to back, so their latencies overlap
+__device__ __forceinline__ bool bar_wait3_warp(uint32_t a, uint32_t pa, bool use_a, uint32_t b, uint32_t pb,
+                                               bool use_b, uint32_t c, uint32_t pc, bool use_c,
+                                               volatile int* abort_flag, int* err) {
+  for (uint32_t i = 0; i < WAIT_LIMIT; ++i) {
+    const bool da = !use_a || bar_test(a, pa);
+    const bool db = !use_b || bar_test(b, pb);
+    const bool dc = !use_c || bar_test(c, pc);
+    if (__all_sync(0xffffffffu, da && db && dc)) return true;
+    if (__any_sync(0xffffffffu, *abort_flag != 0)) return false;
+    // not all complete: suspend on the first pending phase instead of spinning (a spinning
+    // warp takes issue slots from the warps it shares a scheduler with)
+    if (!da) bar_try(a, pa);
+    else if (!db) bar_try(b, pb);
+    else bar_try(c, pc);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    *abort_flag = 1;
+    atomicExch(err, 4);
+  }
+  __syncwarp();
+  return false;
+}
 // bounded wait by a whole converged warp: every lane leaves on the same poll
 __device__ __forceinline__ bool bar_wait_warp(uint32_t a, uint32_t parity, volatile int* abort_flag, int* err) {
   for (uint32_t i = 0; i < WAIT_LIMIT; ++i) {
@@ -62,6 +96,13 @@ __device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 
+// prefetch of a 2-D tile into L2 (no shared memory, no barrier)
+__device__ __forceinline__ void tma_prefetch_2d(const CUtensorMap* map, int x, int y) {
+  asm volatile("cp.async.bulk.prefetch.tensor.2d.L2.global.tile [%0, {%1, %2}];" ::"l"(
+                   reinterpret_cast<uint64_t>(map)),
+               "r"(x), "r"(y)
+               : "memory");
+}
 __device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map, int x, int y, uint32_t bar) {
   asm volatile(
       "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
@@ -106,6 +147,16 @@ __device__ __forceinline__ void mma_bf16_warp(uint32_t tmem_d, uint64_t a, uint6
       "l"(a), "l"(b), "r"(id), "r"(acc)
       : "memory");
 }
+// As mma_bf16_warp with the A operand (M lanes x K, two bf16 per 32-bit column, the lower
+// half holding the even k) read from tensor memory at a_tmem instead of shared memory.
+__device__ __forceinline__ void mma_bf16_tmem_a_warp(uint32_t tmem_d, uint32_t a_tmem, uint64_t b, uint32_t id,
+                                                     uint32_t acc) {
+  asm volatile(
+      "{\n\t.reg .pred p, e;\n\telect.sync _|e, 0xffffffff;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+      "@e tcgen05.mma.cta_group::1.kind::f16 [%0], [%1], %2, %3, p;\n\t}" ::"r"(tmem_d),
+      "r"(a_tmem), "l"(b), "r"(id), "r"(acc)
+      : "memory");
+}
 __device__ __forceinline__ void mma_commit_warp(uint32_t bar) {
   asm volatile(
       "{\n\t.reg .pred e;\n\telect.sync _|e, 0xffffffff;\n\t"
@@ -145,6 +196,17 @@ __device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
   __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
   return *reinterpret_cast<uint32_t*>(&h);
 }
+// TMEM store of 16 columns (one 32-bit value per lane and column); tmem_wait_st before the
+// values may be consumed by another thread or the tensor pipe
+__device__ __forceinline__ void tmem_st16(uint32_t taddr, const uint32_t (&r)[16]) {
+  asm volatile(
+      "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16};" ::"r"(
+          taddr),
+      "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]), "r"(r[7]), "r"(r[8]), "r"(r[9]),
+      "r"(r[10]), "r"(r[11]), "r"(r[12]), "r"(r[13]), "r"(r[14]), "r"(r[15])
+      : "memory");
+}
+__device__ __forceinline__ void tmem_wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
 // asynchronous TMEM load of 16 columns; the registers are valid only after tmem_wait16
 __device__ __forceinline__ void tmem_ld16u(uint32_t taddr, uint32_t (&r)[16]) {
   asm volatile(
