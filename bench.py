@@ -406,7 +406,7 @@ def main():
     # ncu capture summarised in profiles/ (logreg_tc_kernel / logreg_simt_kernel, 1024 chains)
     traffic = None
     if X.shape == (581012, 55) and C == 1024:
-        traffic = 76.69e6 if precision == "bf16x3" else 135.3e6
+        traffic = 77.08e6 if precision == "bf16x3" else 135.3e6
     roofline = {"bound": "tensor", "achieved": achieved, "peak": burst, "unit": "TFLOP/s",
                 "frac": achieved / burst, "traffic": traffic, "traffic_unit": "bytes per launch (ncu capture)",
                 "peak_kind": peak_kind + " burst bf16",
