@@ -159,39 +159,38 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) hs_tc_gemm_kernel(const __grid
     }
   } else if (warp == 1) {
     // ------------------------------------------------------------ MMA issuer
-    if (lane == 0) {
-      constexpr uint32_t ID = idesc(TM, TN, 0, 0);  // both operands K-major
-      constexpr int kPairA[NPAIRS] = {0, 0, 1, 0, 2, 1};
-      constexpr int kPairB[NPAIRS] = {0, 1, 0, 2, 0, 1};
-      const uint32_t base = smem_u32(smem);
-      for (int i = 0; i < nkb; ++i) {
-        const int s = i % STAGES, hb = i & 1;
-        if (!bar_wait(full(s), (i / STAGES) & 1, abort_flag, G.err)) break;
-        if (i >= 2 && !bar_wait(hempty(hb), ((i >> 1) - 1) & 1, abort_flag, G.err)) break;
-        tc_fence_after();
-        const uint32_t st = base + s * STAGE_BYTES;
+    // The whole warp runs the loop and one elected lane issues each MMA and commit (issued by
+    // lane 0 alone, every tcgen05.mma paid a long issue latency); the stage descriptors are built
+    // once and moved by constant offsets.
+    constexpr uint32_t ID = idesc(TM, TN, 0, 0);  // both operands K-major
+    constexpr int kPairA[NPAIRS] = {0, 0, 1, 0, 2, 1};
+    constexpr int kPairB[NPAIRS] = {0, 1, 0, 2, 0, 1};
+    const uint64_t d0 = sdesc(smem_u32(smem), 16, 1024);  // stage 0, offset 0
+    for (int i = 0; i < nkb; ++i) {
+      const int s = i % STAGES, hb = i & 1;
+      if (!bar_wait_warp(full(s), (i / STAGES) & 1, abort_flag, G.err)) break;
+      if (i >= 2 && !bar_wait_warp(hempty(hb), ((i >> 1) - 1) & 1, abort_flag, G.err)) break;
+      tc_fence_after();
+      const uint64_t st = sdesc_at(d0, (uint32_t)(s * STAGE_BYTES));
 #pragma unroll
-        for (int kk = 0; kk < TK / 16; ++kk) {  // hh of this block into its own accumulator
-          const uint64_t a = sdesc(st + kk * 32, 16, 1024);
-          const uint64_t b = sdesc(st + NSPL * A_SPLIT + kk * 32, 16, 1024);
-          mma_bf16(tmem + (uint32_t)(hb * TN), a, b, ID, kk > 0 ? 1u : 0u);
-        }
-        mma_commit(hfull(hb));
+      for (int kk = 0; kk < TK / 16; ++kk)  // hh of this block into its own accumulator
+        mma_bf16_warp(tmem + (uint32_t)(hb * TN), sdesc_at(st, kk * 32), sdesc_at(st, NSPL * A_SPLIT + kk * 32), ID,
+                      kk > 0 ? 1u : 0u);
+      mma_commit_warp(hfull(hb));
 #pragma unroll
-        for (int p = 1; p < NPAIRS; ++p) {  // corrections accumulate over the whole K range
+      for (int p = 1; p < NPAIRS; ++p) {  // corrections accumulate over the whole K range
 #pragma unroll
-          for (int kk = 0; kk < TK / 16; ++kk) {
-            const uint64_t a = sdesc(st + kPairA[p] * A_SPLIT + kk * 32, 16, 1024);
-            const uint64_t b = sdesc(st + NSPL * A_SPLIT + kPairB[p] * B_SPLIT + kk * 32, 16, 1024);
-            mma_bf16(tmem + CORR_COL, a, b, ID, (i > 0 || p > 1 || kk > 0) ? 1u : 0u);
-          }
-        }
-        mma_commit(empty(s));
+        for (int kk = 0; kk < TK / 16; ++kk)
+          mma_bf16_warp(tmem + CORR_COL, sdesc_at(st, kPairA[p] * A_SPLIT + kk * 32),
+                        sdesc_at(st, NSPL * A_SPLIT + kPairB[p] * B_SPLIT + kk * 32), ID,
+                        (i > 0 || p > 1 || kk > 0) ? 1u : 0u);
       }
-      mma_commit(done);
-      // every MMA issued by this thread has completed before TMEM can be released
-      for (uint32_t k = 0; k < WAIT_LIMIT && !bar_try(done, 0); ++k) {
-      }
+      mma_commit_warp(empty(s));
+    }
+    __syncwarp();
+    mma_commit_warp(done);
+    // every MMA issued by this warp has completed before TMEM can be released
+    for (uint32_t k = 0; k < WAIT_LIMIT && !bar_try(done, 0); ++k) {
     }
   } else {
     // ------------------------------------------------------------ epilogue (warps 2..5)
