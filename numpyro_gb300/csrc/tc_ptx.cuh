@@ -1,7 +1,8 @@
 // tc_ptx.cuh -- inline-PTX building blocks of the tcgen05 kernels (logreg_tc.cu, horseshoe_tc.cu):
-// mbarriers with bounded waits, TMA 2-D tile loads, shared-memory matrix descriptors, the
-// kind::f16 instruction descriptor, tcgen05.mma / commit, TMEM loads, and the approximate
-// special functions of the logistic epilogue.
+// mbarriers with bounded waits (single thread and whole warp), TMA 2-D tile loads and L2
+// prefetches, shared-memory matrix descriptors, the kind::f16 instruction descriptor,
+// warp-issued tcgen05.mma / commit (A from shared memory or from TMEM), TMEM loads and stores,
+// and the approximate special functions of the logistic epilogue.
 #pragma once
 #include <cuda.h>
 #include <cuda_bf16.h>
@@ -130,16 +131,10 @@ __host__ __device__ constexpr uint32_t idesc(int M, int N, int a_mn_major, int b
   return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)a_mn_major << 15) | ((uint32_t)b_mn_major << 16) |
          ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
 }
-__device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t id, uint32_t acc) {
-  asm volatile(
-      "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
-      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem_d),
-      "l"(a), "l"(b), "r"(id), "r"(acc)
-      : "memory");
-}
-// The same, executed by a whole converged warp: one elected lane issues the MMA.  Issuing from
-// a converged warp keeps the descriptor arithmetic warp-uniform; from inside `if (lane == 0)`
-// every MMA cost ~70-90 cycles of issue latency.
+// tcgen05.mma (kind::f16, one CTA, D in TMEM, A and B from shared-memory descriptors; acc = 0
+// overwrites D), executed by a whole converged warp: one elected lane issues the MMA.  Issuing
+// from a converged warp keeps the descriptor arithmetic warp-uniform; from inside
+// `if (lane == 0)` every MMA cost ~70-90 cycles of issue latency.
 __device__ __forceinline__ void mma_bf16_warp(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t id, uint32_t acc) {
   asm volatile(
       "{\n\t.reg .pred p, e;\n\telect.sync _|e, 0xffffffff;\n\tsetp.ne.b32 p, %4, 0;\n\t"
@@ -163,9 +158,6 @@ __device__ __forceinline__ void mma_commit_warp(uint32_t bar) {
       "@e tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n\t}" ::"r"(bar)
       : "memory");
 }
-__device__ __forceinline__ void mma_commit(uint32_t bar) {
-  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
-}
 __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
   uint32_t r[16];
   asm volatile(
@@ -185,11 +177,6 @@ __device__ __forceinline__ float ex2_approx(float x) {
 __device__ __forceinline__ float lg2_approx(float x) {
   float y;
   asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
-  return y;
-}
-__device__ __forceinline__ float rcp_approx(float x) {
-  float y;
-  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
   return y;
 }
 __device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
