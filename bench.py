@@ -16,6 +16,7 @@ import ctypes
 import json
 import os
 import subprocess
+import tempfile
 import sys
 import time
 
@@ -203,7 +204,8 @@ class Clocks:
     def __init__(self, gpu):
         self.gpu = gpu
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", "clocks_bench.csv")
+        # raw samples (summarised in the JSON line); GBN_CLOCKS_CSV keeps them somewhere else
+        self.path = os.environ.get("GBN_CLOCKS_CSV", os.path.join(tempfile.gettempdir(), "gbn_clocks_bench.csv"))
 
     def start(self):
         try:
