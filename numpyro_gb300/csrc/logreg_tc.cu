@@ -64,7 +64,7 @@ constexpr int OFF_MISC = OFF_B + NSPLIT * B_TILE;
 constexpr int NUM_BARS = 2 * STAGES + 3 * NBUF + 1;
 constexpr int SMEM_BYTES = OFF_MISC + 256 + BN * 8 + 1024;  // + alignment slack
 constexpr int EPI_WARPS = 16;             // epilogue warps: 4 per TMEM lane quadrant
-constexpr int EPI_GROUP = EPI_WARPS / 2;  // warps that share one tile (one accumulator buffer)
+constexpr int EPI_GROUP = EPI_WARPS / 2;  // warps that share one tile (groups take alternate tiles)
 constexpr int GCOLS = BK * 4 / EPI_WARPS; // gradient columns read back per epilogue warp
 constexpr int NUM_THREADS = 32 * (2 + EPI_WARPS);
 constexpr uint32_t TMEM_COLS = 512;
