@@ -222,6 +222,17 @@ class MCMC:
         out = {k: v for k, v in self._states.items() if k != self._sample_field}
         return out if group_by_chain else {k: self._flat(v) for k, v in out.items()}
 
+    def transfer_states_to_host(self):
+        """Collected states as host arrays (mcmc.py:799-804).  The device run already copies its
+        draws to host memory once, at the end; this converts anything still on the device (a
+        postprocess_fn may return tensors).  last_state stays on the device, to resume from."""
+        def conv(x):
+            return {k: conv(v) for k, v in x.items()} if isinstance(x, dict) else _to_numpy(x)
+
+        if self._states is not None:
+            self._states = conv(self._states)
+        self._states_flat = None
+
     def print_summary(self, prob=0.9, exclude_deterministic=True):
         """(mcmc.py:769-797)"""
         sites = self._states[self._sample_field]

@@ -152,3 +152,20 @@ def test_bf16_rounding_exact():
     r = _round_bf16(a)
     assert np.all((r.view(np.uint32) & 0xFFFF) == 0)
     assert np.max(np.abs(r - a) / np.abs(a)) <= 2.0 ** -8
+
+
+def test_transfer_states_to_host_converts_tensors():
+    """MCMC.transfer_states_to_host (numpyro/infer/mcmc.py:799-804) leaves host arrays only."""
+    import torch
+
+    from numpyro_gb300.mcmc import MCMC
+
+    class _Kernel:
+        sample_field = "z"
+        default_fields = ("z", "diverging")
+
+    m = MCMC(_Kernel(), num_warmup=1, num_samples=2, num_chains=2)
+    m._states = {"z": {"mu": torch.zeros(2, 2), "tau": np.ones((2, 2))}, "diverging": torch.zeros(2, 2)}
+    m.transfer_states_to_host()
+    assert isinstance(m._states["z"]["mu"], np.ndarray) and isinstance(m._states["diverging"], np.ndarray)
+    assert m.get_samples()["mu"].shape == (4,)
