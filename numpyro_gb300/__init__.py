@@ -9,9 +9,10 @@ adjoints run in CUDA kernels of ``libgbnuts.so`` behind a C ABI
 (include/gbnuts.h).  There is no CPU fallback.
 """
 from . import datasets, diagnostics, models
-from .hmc import HMC, NUTS, HMCAdaptState, HMCState, init_to_uniform
+from .hmc import HMC, NUTS, HMCAdaptState, HMCState, hmc, init_to_uniform
 from .mcmc import MCMC, MCMCKernel
+from .util import fori_collect
 
-__all__ = ["HMC", "NUTS", "MCMC", "MCMCKernel", "HMCState", "HMCAdaptState", "init_to_uniform", "models",
-           "datasets", "diagnostics"]
+__all__ = ["HMC", "NUTS", "MCMC", "MCMCKernel", "HMCState", "HMCAdaptState", "hmc", "fori_collect",
+           "init_to_uniform", "models", "datasets", "diagnostics"]
 __version__ = "0.1.0"

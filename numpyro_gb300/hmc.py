@@ -402,3 +402,64 @@ class NUTS(HMC):
                          num_chains=num_chains)
         self._max_tree_depth = max_tree_depth
         self._algo = "NUTS"
+
+
+def hmc(potential_fn=None, kinetic_fn=None, algo="NUTS", *, engine="fused", precision="fp32", num_chains=None):
+    """The functional API (numpyro/infer/hmc.py:113-538): returns ``(init_kernel, sample_kernel)``.
+
+    ``potential_fn`` is a registry model (numpyro_gb300.models), passed where numpyro takes the
+    traced ``model_info.potential_fn``; any other callable raises NotImplementedError, as the
+    kernel classes do.  ``init_kernel`` takes numpyro's arguments (hmc.py:193-212) and builds the
+    NUTS or HMC kernel that ``sample_kernel`` then steps (hmc.py:459-530).  ``init_params`` is
+    None (init_to_uniform on the device), an array of unconstrained values ([D] or [C, D]) or an
+    object with a ``.z`` array such as numpyro's ParamInfo.  ``rng_key`` is an int seed, a key or
+    a [C, 2] batch of keys; C chains run vectorized, one when a single key is given and
+    ``num_chains`` is None.
+    """
+    if algo not in ("HMC", "NUTS"):
+        raise ValueError("`algo` must be one of `HMC` or `NUTS`.")
+    if potential_fn is None:
+        raise ValueError("potential_fn (a numpyro_gb300.models registry model) is required")
+    if not isinstance(potential_fn, Model):
+        raise NotImplementedError(
+            "the GB300 engine evaluates registry potentials only; pass a numpyro_gb300.models model")
+    if kinetic_fn is not None:
+        raise NotImplementedError("only the Euclidean kinetic energy is supported")
+    model = potential_fn
+    holder = {}
+
+    def init_kernel(init_params, num_warmup, step_size=1.0, inverse_mass_matrix=None, adapt_step_size=True,
+                    adapt_mass_matrix=True, dense_mass=False, target_accept_prob=0.8, *, num_steps=None,
+                    trajectory_length=2 * math.pi, max_tree_depth=10, find_heuristic_step_size=False,
+                    forward_mode_differentiation=False, regularize_mass_matrix=True, model_args=(),
+                    model_kwargs=None, rng_key=None):
+        common = dict(model=model, step_size=step_size, inverse_mass_matrix=inverse_mass_matrix,
+                      adapt_step_size=adapt_step_size, adapt_mass_matrix=adapt_mass_matrix, dense_mass=dense_mass,
+                      target_accept_prob=target_accept_prob, find_heuristic_step_size=find_heuristic_step_size,
+                      forward_mode_differentiation=forward_mode_differentiation,
+                      regularize_mass_matrix=regularize_mass_matrix, engine=engine, precision=precision,
+                      num_chains=num_chains)
+        if algo == "NUTS":
+            kernel = NUTS(max_tree_depth=max_tree_depth, **common)
+        else:
+            kernel = HMC(num_steps=num_steps, trajectory_length=trajectory_length, **common)
+        old = holder.pop("kernel", None)
+        if old is not None:
+            old.close()
+        holder["kernel"] = kernel
+        key = 0 if rng_key is None else rng_key
+        z0 = getattr(init_params, "z", init_params)
+        if z0 is not None:
+            z0 = np.asarray(z0.detach().cpu() if hasattr(z0, "detach") else z0, np.float32)
+            if z0.ndim == 1:  # one starting point for every chain
+                C = seed_from_key(key)[1] or num_chains or 1
+                z0 = np.broadcast_to(z0, (C, z0.shape[0]))
+        return kernel.init(key, num_warmup, z0)
+
+    def sample_kernel(hmc_state, model_args=(), model_kwargs=None):
+        if "kernel" not in holder:
+            raise RuntimeError("call init_kernel before sample_kernel")
+        return holder["kernel"].sample(hmc_state)
+
+    init_kernel.kernel = lambda: holder.get("kernel")  # the kernel object behind the closures
+    return init_kernel, sample_kernel

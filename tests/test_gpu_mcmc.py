@@ -124,3 +124,26 @@ def test_logistic_bf16x3_engine_posterior():
     ok, m1, m2, mcse = _mcse_ok(res["bf16x3"], res["fp32"])
     assert ok.mean() >= 0.85, (m1, m2, mcse)
     assert np.all(diagnostics.split_gelman_rubin(res["bf16x3"]) < 1.02)
+
+
+@pytest.mark.gpu
+def test_functional_hmc_api_matches_the_kernel_class():
+    """hmc(potential, algo="NUTS") + fori_collect (numpyro/infer/hmc.py:113, numpyro/util.py:321),
+    as examples/stochastic_volatility.py drives it, gives the NUTS class's draws bit for bit."""
+    from numpyro_gb300 import NUTS, datasets, fori_collect, hmc, models
+
+    ys, ss = datasets.eight_schools(0)
+    model = models.HierarchicalNormal(ys, ss)
+    init_kernel, sample_kernel = hmc(model, algo="NUTS", num_chains=4)
+    st = init_kernel(None, 0, step_size=0.3, adapt_step_size=False, adapt_mass_matrix=False, rng_key=2024)
+    draws = fori_collect(1, 4, sample_kernel, st, transform=lambda s: s.z)
+    k = NUTS(model, num_chains=4, step_size=0.3, adapt_step_size=False, adapt_mass_matrix=False)
+    s = k.init(2024, 0)
+    ref = []
+    for _ in range(4):
+        s = k.sample(s)
+        ref.append(s.z.cpu().numpy())
+    assert draws.shape == (3, 4, model.latent_dim)
+    np.testing.assert_array_equal(draws, np.stack(ref[1:]))
+    k.close()
+    init_kernel.kernel().close()
