@@ -11,8 +11,8 @@ adjoints run in CUDA kernels of ``libgbnuts.so`` behind a C ABI
 from . import datasets, diagnostics, models
 from .hmc import HMC, NUTS, HMCAdaptState, HMCState, hmc, init_to_uniform
 from .mcmc import MCMC, MCMCKernel
-from .util import fori_collect
+from .util import ModelInfo, ParamInfo, fori_collect, initialize_model
 
 __all__ = ["HMC", "NUTS", "MCMC", "MCMCKernel", "HMCState", "HMCAdaptState", "hmc", "fori_collect",
-           "init_to_uniform", "models", "datasets", "diagnostics"]
+           "initialize_model", "ModelInfo", "ParamInfo", "init_to_uniform", "models", "datasets", "diagnostics"]
 __version__ = "0.1.0"

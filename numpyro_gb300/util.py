@@ -1,4 +1,7 @@
-"""Host utilities of numpyro's util module that the functional API needs."""
+"""Host pieces of numpyro's functional API: fori_collect (numpyro/util.py) and initialize_model
+(numpyro/infer/util.py)."""
+from collections import namedtuple
+
 import numpy as np
 
 
@@ -64,3 +67,30 @@ def fori_collect(lower, upper, body_fun, init_val, transform=lambda x: x, progba
         if idx >= 0:
             _tree_set(collection, idx, transform(val))
     return (collection, val) if return_last_val else collection
+
+
+# numpyro/infer/util.py:47-50
+ModelInfo = namedtuple("ModelInfo", ["param_info", "potential_fn", "postprocess_fn", "model_trace"])
+ParamInfo = namedtuple("ParamInfo", ["z", "potential_energy", "z_grad"])
+
+
+def initialize_model(rng_key, model, *, init_strategy=None, dynamic_args=False, model_args=(), model_kwargs=None,
+                     forward_mode_differentiation=False, validate_grad=True):
+    """numpyro.infer.util.initialize_model (numpyro/infer/util.py:663) for a registry model.
+
+    Returns ``ModelInfo(param_info, potential_fn, postprocess_fn, model_trace)`` for the functional
+    API: ``potential_fn`` is the model itself (what ``hmc`` takes), ``postprocess_fn`` maps
+    unconstrained [..., D] values to the constrained sites, and ``param_info.z`` is None, which
+    makes ``init_kernel`` draw init_to_uniform(radius=2) starting points on the device with the
+    reference's retries (numpyro/infer/util.py:366-508).  There is no model trace (None).
+    """
+    from .hmc import init_to_uniform
+    from .models import Model
+
+    if not isinstance(model, Model):
+        raise NotImplementedError("the GB300 engine runs registry models only (numpyro_gb300.models)")
+    if init_strategy is not None and init_strategy is not init_to_uniform:
+        raise NotImplementedError("only init_to_uniform(radius=2) runs on the device")
+    if dynamic_args:
+        raise NotImplementedError("registry models carry their data; dynamic_args is not supported")
+    return ModelInfo(ParamInfo(None, None, None), model, model.postprocess, None)

@@ -110,3 +110,38 @@ def test_hmc_functional_api_rejects_what_the_engine_cannot_run():
     _, sample_kernel = hmc(model)
     with pytest.raises(RuntimeError):
         sample_kernel(None)
+
+
+def test_initialize_model_feeds_the_functional_api(monkeypatch):
+    """The flow of examples/stochastic_volatility.py:90-107 with a registry model: initialize_model
+    -> hmc(model_info.potential_fn) -> init_kernel(model_info.param_info) -> fori_collect with
+    postprocess_fn (the device calls stubbed)."""
+    import torch
+
+    from numpyro_gb300 import HMC, fori_collect, hmc, initialize_model, models
+
+    T = 6
+    model = models.StochasticVolatility(np.linspace(-0.01, 0.01, T))
+    info = initialize_model(0, model, model_args=())
+    assert info.potential_fn is model and info.param_info.z is None and info.model_trace is None
+
+    class _S:
+        def __init__(self, z):
+            self.z = z
+
+    seen = {}
+
+    def fake_init(self, rng_key, num_warmup, init_params=None, model_args=(), model_kwargs={}):
+        seen["init_params"] = init_params
+        return _S(torch.zeros(1, model.latent_dim))
+
+    monkeypatch.setattr(HMC, "init", fake_init)
+    monkeypatch.setattr(HMC, "sample", lambda self, s, model_args=(), model_kwargs={}: _S(s.z + 0.1))
+    init_kernel, sample_kernel = hmc(info.potential_fn, algo="NUTS")
+    state = init_kernel(info.param_info, 3, rng_key=1)
+    assert seen["init_params"] is None  # no starting point: drawn on the device
+    out = fori_collect(3, 5, sample_kernel, state, transform=lambda s: info.postprocess_fn(s.z.numpy()))
+    assert sorted(out) == ["h", "nu", "s"] and out["h"].shape == (2, 1, T)
+    np.testing.assert_allclose(out["s"][:, 0, 0], np.exp([0.4, 0.5]), rtol=1e-6)
+    with pytest.raises(NotImplementedError):
+        initialize_model(0, lambda: None)
