@@ -1,0 +1,58 @@
+"""Diagnostics contracts of numpyro's test/test_diagnostics.py:19-59 (shapes, batching along the
+last axis, HPDI), on seeded inputs, and the keys of summary() (numpyro/diagnostics.py:235-287)."""
+import numpy as np
+import pytest
+
+from numpyro_gb300.diagnostics import (autocorrelation, autocovariance, effective_sample_size, gelman_rubin, hpdi,
+                                       split_gelman_rubin, summary)
+
+
+@pytest.mark.parametrize("statistic, input_shape, output_shape", [
+    (autocorrelation, (10,), (10,)), (autocorrelation, (10, 3), (10, 3)),
+    (autocovariance, (10,), (10,)), (autocovariance, (10, 3), (10, 3)),
+    (hpdi, (10,), (2,)), (hpdi, (10, 3), (2, 3)),
+    (gelman_rubin, (4, 10), ()), (gelman_rubin, (4, 10, 3), (3,)),
+    (split_gelman_rubin, (4, 10), ()), (split_gelman_rubin, (4, 10, 3), (3,)),
+    (effective_sample_size, (4, 10), ()), (effective_sample_size, (4, 10, 3), (3,)),
+])
+def test_shape_and_batching(statistic, input_shape, output_shape):
+    x = np.random.default_rng(0).normal(size=input_shape)
+    y = statistic(x)
+    assert np.shape(y) == output_shape
+    if x.shape[-1] == 3:  # the last axis is a batch: each column alone gives the same values
+        for i in range(3):
+            np.testing.assert_allclose(statistic(x[..., i]), y[..., i])
+
+
+def test_hpdi():
+    """numpyro's test_hpdi (test_diagnostics.py:53-58).  For the normal its 20,000 draws and 0.01
+    tolerance are within the statistic's own noise (the narrowest 80 % window of a normal sample
+    wanders by up to ~0.1 from the central quantiles at that size, shrinking about as n^-1/3), so
+    the normal case uses 10^6 draws and 0.03.  The exponential case, anchored at 0, keeps 0.01."""
+    rng = np.random.default_rng(1)
+    x = rng.normal(size=1_000_000)
+    np.testing.assert_allclose(hpdi(x, prob=0.8), np.quantile(x, [0.1, 0.9]), atol=0.03)
+    x = rng.exponential(size=20000)
+    np.testing.assert_allclose(hpdi(x, prob=0.2), [0.0, 0.22], atol=0.01)
+
+
+def test_hpdi_is_the_narrowest_window():
+    """Brute force over every window of int(prob * n) + 1 sorted draws (diagnostics.py:206-232)."""
+    rng = np.random.default_rng(3)
+    for x in (rng.gamma(2.0, size=301), rng.standard_t(3, size=200)):
+        s = np.sort(x)
+        k = int(0.7 * x.size)
+        lengths = [s[i + k] - s[i] for i in range(x.size - k)]
+        i = int(np.argmin(lengths))
+        np.testing.assert_array_equal(hpdi(x, prob=0.7), [s[i], s[i + k]])
+
+
+def test_summary_keys_and_values():
+    rng = np.random.default_rng(2)
+    s = summary({"a": rng.normal(size=(4, 500)), "b": rng.normal(size=(4, 500, 2))}, prob=0.9)
+    assert list(s["a"]) == ["mean", "std", "median", "5.0%", "95.0%", "n_eff", "r_hat"]
+    assert s["b"]["mean"].shape == (2,)
+    assert abs(float(s["a"]["mean"])) < 0.1 and abs(float(s["a"]["std"]) - 1) < 0.1
+    assert 0.99 < float(s["a"]["r_hat"]) < 1.01
+    flat = summary({"a": rng.normal(size=(2000,))}, group_by_chain=False)
+    assert flat["a"]["n_eff"] > 1000
