@@ -299,7 +299,7 @@ def run_reference(args):
                       budget_s=150.0)
     line = {"metric": METRIC, "value": cb["value"], "unit": "ESS/s", "impl": "reference", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * cb["sampling_s"] / max(1, args.steps),
-            "higher_is_better": True, "dtype": "f32", "data": "synthetic",
+            "higher_is_better": True, "scaling": "weak", "dtype": "f32", "data": "synthetic",
             "config": {"workload": WORKLOAD, "chains_timed": chains, "iters_per_step": per_step},
             "cpu_baseline": cb,
             "e2e": {"value": cb["value"], "unit": "ESS/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
