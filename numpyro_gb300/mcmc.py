@@ -2,7 +2,8 @@
 
 ``MCMCKernel`` restates the plugin ABC (mcmc.py:33-159).  ``MCMC`` restates
 the driver's public surface -- run / warmup / get_samples / get_extra_fields /
-print_summary / post_warmup_state / last_state (mcmc.py:225-809) -- for
+print_summary / post_warmup_state / last_state / transfer_states_to_host
+(mcmc.py:225-809) -- for
 ``chain_method="vectorized"``.  With a GB300 kernel (numpyro_gb300.HMC/NUTS)
 the whole warmup+sampling loop runs on the device in one gbn_run call (the
 analogue of fori_collect's single compiled loop, numpyro/util.py:321-454);
@@ -156,15 +157,16 @@ class MCMC:
         self._last_state = last
 
     def _run_device(self, rng_key, args, kwargs, fields, init_params, n_iter, lower):
-        torch = __import__("torch")
-        from .hmc import HMC
+        import torch
+
+        from .hmc import HMC, seed_from_key
 
         kernel = self.sampler
         if kernel._num_chains is None:
             kernel._num_chains = self.num_chains
         if self._warmup_state is not None:
             state = HMC.copy_state(self._warmup_state)
-            seed, _ = __import__("numpyro_gb300.hmc", fromlist=["seed_from_key"]).seed_from_key(rng_key)
+            seed, _ = seed_from_key(rng_key)
             kernel._ensure_handle(state.z.shape[0], kernel._handle_key[1] if kernel._handle_key else seed)
         else:
             state = kernel.init(rng_key, self.num_warmup, init_params, args, kwargs)
