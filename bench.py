@@ -465,7 +465,9 @@ def _tc_available():
 
 
 def _launches_per_tick(precision):
-    return 2 if precision == "bf16x3" else 3  # advance + potential kernels
+    # advance_kernel, then the potential: split_coefs + logreg_tc + logreg_finish on the tensor
+    # cores, logreg_simt + logreg_finish on CUDA cores (the launch list in profiles/ shows the four)
+    return 4 if precision == "bf16x3" else 3
 
 
 def _time_potential(kernel, state, reps=10):
