@@ -164,7 +164,8 @@ int gbn_latent_dim(gbn_handle h, int32_t* dim);
 /* U(z) and dU/dz for num_points latent vectors (device pointers). */
 int gbn_potential_and_grad(gbn_handle h, void* stream, const float* d_z, int32_t num_points,
                            double* d_pe, float* d_grad);
-/* Vector-Jacobian product of U: d_out = cot[k] * dU/dz(z_k). */
+/* Vector-Jacobian product of U: d_out = cot[k] * dU/dz(z_k).  Allocates nothing when
+ * num_points <= num_chains (the handle's scratch is sized for that many points at gbn_create). */
 int gbn_potential_vjp(gbn_handle h, void* stream, const float* d_z, int32_t num_points,
                       const double* d_cot, float* d_out);
 
@@ -193,15 +194,16 @@ const char* gbn_tuning(gbn_handle h);
 
 /* Logistic-regression U(z) and dU/dz (FP32 CUDA cores, same arithmetic as the
  * LOGREG family) that allocates no device memory, for callers that cannot call
- * cudaMalloc: a JAX/XLA FFI handler (XLA owns the device buffers), code running
- * inside a CUDA stream capture, hosts that manage all memory in their own pool.
+ * cudaMalloc: a JAX/XLA FFI handler (XLA owns the device buffers and must not see
+ * allocations per call), hosts that manage all device memory in their own pool.
  * No counterpart in the reference.  d_x [n][p] row-major, d_y [n], d_z
  * [num_points][p], d_pe [num_points], d_grad [num_points][p]; requires
- * 1 <= num_points <= GBN_NOALLOC_MAX_POINTS and 1 <= p <= 64, else
- * GBN_ERR_INVALID_ARG.  Its scratch is a static device array of about 1 MB that
- * every GPU loading the library holds until exit, shared by all calls: calls
- * that overlap on the GPU race and must be serialised by the caller.  The first
- * call on a device performs the set-up and should come before any stream capture. */
+ * 1 <= num_points <= GBN_NOALLOC_MAX_POINTS, 1 <= p <= 64 and a finite
+ * prior_scale > 0, else GBN_ERR_INVALID_ARG.  Its scratch is a static device
+ * array of about 1 MB that every GPU loading the library holds until exit, shared
+ * by all calls: calls that overlap on the GPU race and must be serialised by the
+ * caller.  The first call on a device performs the set-up (symbol addresses, the
+ * kernel's shared-memory limit) and should come before any stream capture. */
 int gbn_logreg_potential_noalloc(void* stream, const float* d_x, const float* d_y, int64_t n, int32_t p,
                                  double prior_scale, const float* d_z, int32_t num_points, double* d_pe,
                                  float* d_grad);

@@ -50,6 +50,8 @@ struct gbn_handle_s {
   cudaGraphExec_t tick_graph = nullptr;
   void* graph_scratch = nullptr;  // potential scratch the graph was captured with
   std::string tuning;             // launch shapes chosen by the autotuner
+  double* vjp_pe = nullptr;       // potential values discarded by gbn_potential_vjp
+  int vjp_cap = 0;
 };
 
 static thread_local std::string g_last_error;
@@ -348,6 +350,8 @@ int gbn_create(gbn_handle* out, const gbn_model_desc* md, const gbn_config* cfg)
   if (ce == cudaSuccess) ce = dalloc(h, &h->flags, (size_t)C);
   if (ce == cudaSuccess) ce = dalloc(h, &h->err_word, 4);
   if (ce == cudaSuccess) ce = dalloc(h, &h->dP, 1);
+  if (ce == cudaSuccess) ce = dalloc(h, &h->vjp_pe, (size_t)C);
+  h->vjp_cap = C;
   if (ce == cudaSuccess) ce = cudaMallocHost((void**)&h->h_counters, sizeof(int32_t) * 8);
   if (ce == cudaSuccess) ce = cudaEventCreate(&h->ev0);
   if (ce == cudaSuccess) ce = cudaEventCreate(&h->ev1);
@@ -436,12 +440,20 @@ int gbn_potential_vjp(gbn_handle h, void* stream, const float* d_z, int32_t num_
   if (!h || !d_z || !d_cot || !d_out || num_points <= 0)
     return fail(h, GBN_ERR_INVALID_ARG, "gbn_potential_vjp: bad argument");
   cudaStream_t st = (cudaStream_t)stream;
-  double* pe = nullptr;
-  cudaError_t e = cudaMallocAsync(&pe, sizeof(double) * num_points, st);
-  if (e != cudaSuccess) return cuda_fail(h, e, "vjp scratch");
-  e = launch_potential(h->m, d_z, num_points, pe, d_out, nullptr, st);
+  cudaError_t e = cudaSuccess;
+  if (num_points > h->vjp_cap) {  // only for more points than the handle's chains
+    if (h->vjp_pe) {
+      cudaStreamSynchronize(st);
+      cudaFree(h->vjp_pe);
+      h->allocs.erase(std::find(h->allocs.begin(), h->allocs.end(), (void*)h->vjp_pe));
+      h->vjp_pe = nullptr;
+    }
+    e = dalloc(h, &h->vjp_pe, (size_t)num_points);
+    if (e != cudaSuccess) return cuda_fail(h, e, "vjp scratch");
+    h->vjp_cap = num_points;
+  }
+  e = launch_potential(h->m, d_z, num_points, h->vjp_pe, d_out, nullptr, st);
   if (e == cudaSuccess) e = launch_scale_rows(d_cot, d_out, num_points, h->D, st);
-  cudaFreeAsync(pe, st);
   if (e != cudaSuccess) return cuda_fail(h, e, "vjp launch");
   return GBN_OK;
 }

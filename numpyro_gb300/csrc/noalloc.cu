@@ -1,12 +1,11 @@
 // noalloc.cu -- the logistic-regression potential without any device allocation.
 //
-// Some callers cannot call cudaMalloc when they need a potential evaluated:
+// Some callers cannot call cudaMalloc at the moment they need a potential evaluated:
 //   * a JAX/XLA FFI custom-call handler: XLA owns every device buffer of the
 //     computation and, with its default preallocation, leaves little memory
-//     that cudaMalloc could still hand out; a handler must not allocate per call;
-//   * code that runs while a CUDA stream is being captured into a graph, where
-//     a cudaMalloc call is not allowed;
-//   * host frameworks that route all device memory through their own pool.
+//     that cudaMalloc could still hand out, so a handler must not allocate per call;
+//   * host frameworks that route all device memory through their own pool
+//     and forbid allocations behind their back.
 // gbn_logreg_potential_noalloc serves them: the caller passes the data, the
 // positions and the outputs as device pointers, and the kernel's scratch (the
 // per-row-group partial gradients and log-likelihoods of the FP32 logistic
@@ -14,12 +13,13 @@
 // every GPU loading this library holds until the process exits.
 //
 // The first call on a device (with that device current) looks up the device
-// addresses of the arrays with cudaGetSymbolAddress and sets the kernel's
-// shared-memory attribute; make that first call before any stream capture.
-// All calls share the arrays: calls that overlap on the GPU (on different
-// streams, or from different threads) race on them and must be serialised by
-// the caller.  Nothing needs clearing between calls, because every scratch word
-// the kernels read is written earlier in the same call.
+// addresses of the arrays with cudaGetSymbolAddress and raises the kernel's
+// shared-memory limit on that device; make that first call before any stream
+// capture.  All calls share the arrays: calls that overlap on the GPU (on
+// different streams, or from different threads) race on them and must be
+// serialised by the caller.  Nothing needs clearing between calls, because every
+// scratch word the kernels read is written earlier in the same call.
+#include <cmath>
 #include <mutex>
 #include <string>
 
@@ -31,6 +31,7 @@ namespace gbn {
 cudaError_t launch_logreg_simt_scratch(const float* x, const float* y, int64_t n, int p, double prior_scale,
                                        const float* Q, int npts, int row_groups, float* part_g, double* part_ll,
                                        double* PE, float* G, cudaStream_t st);
+cudaError_t logreg_simt_smem_attr();
 
 namespace {
 
@@ -67,6 +68,8 @@ extern "C" int gbn_logreg_potential_noalloc(void* stream, const float* d_x, cons
     return noalloc_fail(GBN_ERR_INVALID_ARG, "gbn_logreg_potential_noalloc: null pointer");
   if (n < 1 || p < 1 || p > 64)
     return noalloc_fail(GBN_ERR_INVALID_ARG, "gbn_logreg_potential_noalloc: need n >= 1 and 1 <= p <= 64");
+  if (!(prior_scale > 0.0) || !std::isfinite(prior_scale))
+    return noalloc_fail(GBN_ERR_INVALID_ARG, "gbn_logreg_potential_noalloc: prior_scale must be finite and > 0");
   if (num_points < 1 || num_points > GBN_NOALLOC_MAX_POINTS)
     return noalloc_fail(GBN_ERR_INVALID_ARG,
                         "gbn_logreg_potential_noalloc: num_points must be in [1, GBN_NOALLOC_MAX_POINTS = " +
@@ -87,6 +90,9 @@ extern "C" int gbn_logreg_potential_noalloc(void* stream, const float* d_x, cons
       e = cudaGetSymbolAddress(&pl, g_noalloc_part_ll);
       if (e != cudaSuccess)
         return noalloc_fail(GBN_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+      e = logreg_simt_smem_attr();
+      if (e != cudaSuccess)
+        return noalloc_fail(GBN_ERR_CUDA, std::string("cudaFuncSetAttribute: ") + cudaGetErrorString(e));
       g_scratch[dev].part_g = static_cast<float*>(pg);
       g_scratch[dev].part_ll = static_cast<double*>(pl);
     }
@@ -94,7 +100,7 @@ extern "C" int gbn_logreg_potential_noalloc(void* stream, const float* d_x, cons
   }
   int64_t ntiles = (n + 63) / 64;
   int row_groups = (int)(ntiles < kRowGroups ? ntiles : kRowGroups);
-  e = launch_logreg_simt_scratch(d_x, d_y, n, p, prior_scale > 0 ? prior_scale : 1.0, d_z, num_points, row_groups,
+  e = launch_logreg_simt_scratch(d_x, d_y, n, p, prior_scale, d_z, num_points, row_groups,
                                  s.part_g, s.part_ll, d_pe, d_grad, (cudaStream_t)stream);
   if (e != cudaSuccess) return noalloc_fail(GBN_ERR_CUDA, std::string("launch: ") + cudaGetErrorString(e));
   return GBN_OK;

@@ -504,6 +504,27 @@ static size_t logreg_smem(int DP) {
          sizeof(double) * 16 * LR_CT;
 }
 
+namespace {
+std::mutex g_simt_attr_mu;
+std::vector<char> g_simt_attr_done;  // per device ordinal: the shared-memory limit is raised
+}  // namespace
+
+// logreg_simt_kernel needs about 74 KB of dynamic shared memory at 64 features, above the 48 KB
+// default.  The limit is a per-device attribute of the kernel, so it is raised once for every
+// device the kernel runs on (with that device current), under a mutex.
+cudaError_t logreg_simt_smem_attr() {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0) return cudaErrorInvalidDevice;
+  std::lock_guard<std::mutex> lock(g_simt_attr_mu);
+  if ((int)g_simt_attr_done.size() <= dev) g_simt_attr_done.resize((size_t)dev + 1, 0);
+  if (g_simt_attr_done[(size_t)dev]) return cudaSuccess;
+  e = cudaFuncSetAttribute(logreg_simt_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)logreg_smem(64));
+  if (e == cudaSuccess) g_simt_attr_done[(size_t)dev] = 1;
+  return e;
+}
+
 cudaError_t launch_potential(ModelDev& m, const float* Q, int npts, double* PE, float* G, const int32_t* pending,
                              cudaStream_t st) {
   if (npts <= 0) return cudaSuccess;
@@ -523,11 +544,8 @@ cudaError_t launch_potential(ModelDev& m, const float* Q, int npts, double* PE, 
       if (m.precision == 1 && m.tc) return logreg_tc_launch(m, Q, npts, PE, G, pending, st);
       int DP = logreg_dp(m.p);
       size_t sm = logreg_smem(DP);
-      static bool attr_set = false;
-      if (!attr_set) {
-        cudaFuncSetAttribute(logreg_simt_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)logreg_smem(64));
-        attr_set = true;
-      }
+      e = logreg_simt_smem_attr();
+      if (e != cudaSuccess) return e;
       const int rg = m.tune.lr_rg > 0 ? m.tune.lr_rg : m.row_groups;
       dim3 grid((npts + LR_CT - 1) / LR_CT, rg);
       logreg_simt_kernel<<<grid, 256, sm, st>>>(m.x, m.y, m.n, m.p, DP, Q, npts, ld, m.part_g, m.part_ll, rg,
@@ -694,17 +712,14 @@ namespace gbn {
 cudaError_t launch_logreg_simt_scratch(const float* x, const float* y, int64_t n, int p, double prior_scale,
                                        const float* Q, int npts, int row_groups, float* part_g, double* part_ll,
                                        double* PE, float* G, cudaStream_t st) {
-  static bool attr_set = false;
-  if (!attr_set) {
-    cudaError_t e = cudaFuncSetAttribute(logreg_simt_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)logreg_smem(64));
-    if (e != cudaSuccess) return e;
-    attr_set = true;
-  }
+  cudaError_t e = logreg_simt_smem_attr();
+  if (e != cudaSuccess) return e;
   int DP = logreg_dp(p);
   dim3 grid((npts + LR_CT - 1) / LR_CT, row_groups);
   logreg_simt_kernel<<<grid, 256, logreg_smem(DP), st>>>(x, y, n, p, DP, Q, npts, p, part_g, part_ll, row_groups,
                                                          nullptr);
+  e = cudaGetLastError();  // checked per launch, so the first failing launch is the one reported
+  if (e != cudaSuccess) return e;
   logreg_finish_kernel<<<(npts + 7) / 8, 256, 0, st>>>(Q, npts, p, p, row_groups, part_g, part_ll, nullptr,
                                                        prior_scale, PE, G, nullptr);
   return cudaGetLastError();

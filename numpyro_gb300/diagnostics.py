@@ -1,3 +1,9 @@
+# Portions of this file (the estimators from _compute_chain_variance_stats to
+# effective_sample_size) are adapted from numpyro/diagnostics.py of NumPyro,
+# Copyright Contributors to the Pyro project, licensed under the Apache License,
+# Version 2.0 (http://www.apache.org/licenses/LICENSE-2.0).  They are kept
+# statement-for-statement equivalent on purpose: the R-hat gate and the ESS known
+# answers of the benchmark are numpyro's own.
 """MCMC diagnostics (numpyro/diagnostics.py restated, plus rank-normalised bulk ESS).
 
 ``effective_sample_size``, ``split_gelman_rubin``, ``gelman_rubin``,

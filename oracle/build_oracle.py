@@ -54,8 +54,120 @@ def load(prec="f64"):
                                 ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                 ctypes.c_uint64, ctypes.c_int, ctypes.c_int, fp, fp, fp, fp, fp, fp,
                                 ctypes.c_double]
+    mp = ctypes.POINTER(NutsrefModel)
+    lib.nutsref_latent_dim.restype = ctypes.c_int
+    lib.nutsref_latent_dim.argtypes = [mp, ctypes.c_int]
+    lib.nutsref_potential.restype = ctypes.c_double
+    lib.nutsref_potential.argtypes = [mp, ctypes.c_int, fp, fp]
+    lib.nutsref_transitions.restype = ctypes.c_int
+    lib.nutsref_transitions.argtypes = [mp, ctypes.c_int, fp, fp, ctypes.c_int, fp, fp, fp, fp, ctypes.c_uint64,
+                                        ctypes.c_int, ctypes.c_int, fp, fp, fp, fp, fp]
+    lib.nutsref_run_model.restype = ctypes.c_int
+    lib.nutsref_run_model.argtypes = [mp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                      ctypes.c_uint64, ctypes.c_int, ctypes.c_int, fp, fp, fp, fp, fp, fp, fp, fp,
+                                      fp, ctypes.c_double]
     _cache[prec] = lib
     return lib
+
+
+class NutsrefModel(ctypes.Structure):
+    """nutsref_model of nuts_ref.c (the registry model, as gbn_model_desc)."""
+
+    _fields_ = [("family", ctypes.c_int32), ("num_models", ctypes.c_int32), ("chains_per_model", ctypes.c_int32),
+                ("P", ctypes.c_int32), ("N", ctypes.c_int64), ("X", ctypes.c_void_p), ("y", ctypes.c_void_p),
+                ("sigma", ctypes.c_void_p), ("offsets", ctypes.c_void_p), ("hyper", ctypes.c_double * 4)]
+
+
+class Model:
+    """Keeps the arrays of a NutsrefModel alive.  kind: hier_nc, logreg, horseshoe,
+    horseshoe_nc, sv, sv_nc (as oracle.potentials_ref.FAMILIES)."""
+
+    def __init__(self, kind, X=None, y=None, sigma=None, offsets=None, chains_per_model=1, hyper=None):
+        fam = {"hier_nc": 1, "logreg": 2, "horseshoe": 3, "horseshoe_nc": 3, "sv": 4, "sv_nc": 4}[kind]
+        self.kind = kind
+        self.X = None if X is None else np.ascontiguousarray(X, np.float32)
+        self.y = np.ascontiguousarray(y, np.float32)
+        self.sigma = None if sigma is None else np.ascontiguousarray(sigma, np.float32)
+        self.offsets = None if offsets is None else np.ascontiguousarray(offsets, np.int32)
+        h = [0.0] * 4
+        if kind == "hier_nc":
+            h[:2] = [5.0, 5.0]
+        elif kind == "logreg":
+            h[0] = 1.0
+        elif kind == "horseshoe_nc":
+            h[0] = 1.0
+        elif kind in ("sv", "sv_nc"):
+            h[:3] = [10.0, 0.1, 1.0 if kind == "sv_nc" else 0.0]
+        if hyper is not None:
+            h[:len(hyper)] = list(hyper)
+        s = NutsrefModel()
+        s.family = fam
+        s.num_models = 1 if self.offsets is None else len(self.offsets) - 1
+        s.chains_per_model = chains_per_model
+        s.P = 0 if self.X is None else self.X.shape[1]
+        s.N = len(self.y) if fam != 1 or self.offsets is None else int(self.offsets[-1])
+        if fam == 1 and self.offsets is None:
+            s.N = len(self.y)
+        s.X = _p(self.X)
+        s.y = _p(self.y)
+        s.sigma = _p(self.sigma)
+        s.offsets = _p(self.offsets)
+        s.hyper = (ctypes.c_double * 4)(*h)
+        self.struct = s
+
+    def ref(self):
+        return ctypes.byref(self.struct)
+
+
+def potential(lib, model, z, model_index=0):
+    """(U, dU/dz) of one point, from the C restatement (FP64 with the f64 build)."""
+    z = np.ascontiguousarray(z, np.float64)
+    g = np.zeros_like(z)
+    pe = lib.nutsref_potential(model.ref(), model_index, _p(z), _p(g))
+    return pe, g
+
+
+def transitions(lib, model, z0, step, inv, msq, chain_ids, iters, seed, max_tree_depth=10, threads=0):
+    """One NUTS transition per row of z0 (see nutsref_transitions in nuts_ref.c)."""
+    z0 = np.ascontiguousarray(z0, np.float32)
+    C, ld = z0.shape
+    step = np.ascontiguousarray(np.broadcast_to(step, (C,)), np.float32)
+    inv = np.ascontiguousarray(np.broadcast_to(inv, (C, ld)), np.float32)
+    msq = np.ascontiguousarray(np.broadcast_to(msq, (C, ld)), np.float32)
+    ids = np.ascontiguousarray(np.broadcast_to(chain_ids, (C,)), np.uint32)
+    its = np.ascontiguousarray(np.broadcast_to(iters, (C,)), np.uint32)
+    z = np.zeros((C, ld), np.float32)
+    ns = np.zeros(C, np.int32)
+    ap = np.zeros(C, np.float64)
+    dv = np.zeros(C, np.uint8)
+    pe = np.zeros(C, np.float64)
+    lib.nutsref_transitions(model.ref(), C, _p(ids), _p(its), ld, _p(z0), _p(step), _p(inv), _p(msq), int(seed),
+                            max_tree_depth, threads, _p(z), _p(ns), _p(ap), _p(dv), _p(pe))
+    return {"z": z, "num_steps": ns, "accept_prob": ap, "diverging": dv.astype(bool), "potential_energy": pe}
+
+
+def run_model(lib, model, ld, chains, num_warmup, num_samples, seed=0, first_chain=0, max_tree_depth=10, threads=0,
+              init=None, warmup_budget_s=0.0):
+    """Warmup (Stan windows, diagonal mass) + sampling of `chains` chains of `model`."""
+    S = max(num_samples, 0)
+    samples = np.zeros((chains, S, ld), np.float32)
+    nsteps = np.zeros((chains, S), np.int32)
+    div = np.zeros((chains, S), np.uint8)
+    astep = np.zeros(chains, np.float32)
+    ainv = np.zeros((chains, ld), np.float32)
+    timing = np.zeros(5, np.float64)
+    iz = istep = iinv = None
+    if init is not None:
+        iz = np.ascontiguousarray(init[0], np.float32)
+        istep = np.ascontiguousarray(init[1], np.float32)
+        iinv = np.ascontiguousarray(init[2], np.float32)
+    lib.nutsref_run_model(model.ref(), ld, chains, first_chain, num_warmup, num_samples, int(seed), max_tree_depth,
+                          threads, _p(iz), _p(istep), _p(iinv), _p(samples), _p(nsteps), _p(div), _p(astep),
+                          _p(ainv), _p(timing), float(warmup_budget_s))
+    return {"samples": samples, "num_steps": nsteps, "diverging": div.astype(bool), "step_size": astep,
+            "inverse_mass_matrix": ainv, "warmup_s": timing[0], "sampling_s": timing[1],
+            "warmup_grad_evals": timing[2], "sampling_grad_evals": timing[3], "threads": int(timing[4]),
+            "chains": chains}
 
 
 def _p(a):

@@ -8,6 +8,10 @@
  * :961-981, build_tree :1088-1180, dual_averaging :60-130,
  * welford_covariance :133-239, build_adaptation_schedule :387-436,
  * warmup_adapter :518-707; numpyro/infer/hmc.py sample_kernel :459-530.
+ * Potentials follow numpyro's potential_energy (numpyro/infer/util.py:333-358)
+ * for the registry families, as oracle/potentials_ref.py restates them (which
+ * the CPU tests pin to scipy.stats and to central differences; this file is
+ * pinned to that restatement by tests/test_oracle_c.py).
  * Randomness: Philox4x32-10 at the stream addresses of oracle/philox.py.
  *
  * Build: REAL=double (FP64 oracle) or REAL=float (FP32, numpyro's default
@@ -30,6 +34,10 @@
 #define REAL_IS_FLOAT 0
 #endif
 typedef REAL real;
+
+#define LOG_2PI 1.8378770664093453
+#define LOG_PI 1.1447298858494002
+#define LOG_2 0.6931471805599453
 
 /* ------------------------------------------------------------------ Philox */
 static void philox(const uint32_t ctr[4], uint32_t k0, uint32_t k1, uint32_t out[4]) {
@@ -70,22 +78,64 @@ static void normals(seed_t s, uint32_t chain, uint32_t n, uint32_t purpose, int 
   }
 }
 
-/* ------------------------------------------------------------------ potentials */
+/* ------------------------------------------------------------------ models */
+/* The registry model (mirrors gbn_model_desc of include/gbnuts.h):
+ *   family 1  non-centred hierarchical normal; N groups in num_models datasets (offsets),
+ *             chain c runs dataset c / chains_per_model; hyper = (mu scale, tau scale)
+ *   family 2  logistic regression, X [N][P]; hyper[0] = prior scale
+ *   family 3  horseshoe regression, X [N][P]; hyper[0] = 1 selects the non-centred form
+ *   family 4  stochastic volatility, returns y [N = T]; hyper = (s rate, nu rate, non-centred) */
 typedef struct {
-  int family; /* 1 hier_nc, 2 logreg */
+  int32_t family;
+  int32_t num_models;
+  int32_t chains_per_model;
+  int32_t P;
   int64_t N;
-  int D;
   const float* X;
   const float* y;
   const float* sigma;
+  const int32_t* offsets;
   double hyper[4];
-} model_t;
+} nutsref_model;
+
+int nutsref_latent_dim(const nutsref_model* m, int model_index) {
+  switch (m->family) {
+    case 1:
+      if (m->offsets) return m->offsets[model_index + 1] - m->offsets[model_index] + 2;
+      return (int)m->N + 2;
+    case 2: return m->P;
+    case 3: return 2 * m->P + 2;
+    case 4: return (int)m->N + 2;
+    default: return 0;
+  }
+}
+
+static int model_of_chain(const nutsref_model* m, uint32_t chain) {
+  if (m->family != 1 || !m->offsets) return 0;
+  int cpm = m->chains_per_model > 0 ? m->chains_per_model : 1;
+  int k = (int)(chain / (uint32_t)cpm);
+  return k < m->num_models ? k : m->num_models - 1;
+}
+
+/* digamma: upward recurrence to x >= 10, then the asymptotic series
+ * psi(x) ~ ln x - 1/(2x) - sum_k B_2k / (2k x^2k) (Abramowitz & Stegun 6.3.18) */
+static double digamma_ref(double x) {
+  double acc = 0.0;
+  while (x < 10.0) {
+    acc -= 1.0 / x;
+    x += 1.0;
+  }
+  double f = 1.0 / (x * x);
+  double t = f * (-1.0 / 12 + f * (1.0 / 120 + f * (-1.0 / 252 + f * (1.0 / 240 + f * (-1.0 / 132 +
+             f * (691.0 / 32760 + f * (-1.0 / 12)))))));
+  return acc + log(x) - 0.5 / x + t;
+}
 
 /* numpyro potential_energy of the logistic model (examples/covtype.py:66-71):
  * one fused pass over the rows; per-row arithmetic in `real`, sums in double. */
 #define LR_BLOCK 256
-static double logreg_pg(const model_t* m, const real* b, real* g) {
-  int D = m->D;
+static double logreg_pg(const nutsref_model* m, const real* b, real* g) {
+  int D = m->P;
   double ll = 0.0;
   double* ga = (double*)calloc((size_t)D, sizeof(double));
   real* gb = (real*)calloc((size_t)D, sizeof(real));
@@ -126,16 +176,20 @@ static double logreg_pg(const model_t* m, const real* b, real* g) {
   return ll + pr;
 }
 
-/* non-centred hierarchical normal, z = [mu, log tau, theta_base(J)] */
-static double hier_pg(const model_t* m, const real* z, real* g) {
-  int J = (int)m->N;
+/* non-centred hierarchical normal of dataset k, z = [mu, log tau, theta_base(J)]
+ * (potentials_ref.hier_nc_potential / hier_nc_grad) */
+static double hier_pg(const nutsref_model* m, int k, const real* z, real* g) {
+  int j0 = m->offsets ? m->offsets[k] : 0;
+  int J = m->offsets ? m->offsets[k + 1] - j0 : (int)m->N;
+  const float* ys = m->y + j0;
+  const float* ss = m->sigma + j0;
   double ms = m->hyper[0] > 0 ? m->hyper[0] : 5.0, ts = m->hyper[1] > 0 ? m->hyper[1] : 5.0;
   double mu = z[0], lt = z[1], tau = exp(lt);
   double lp = -0.5 * (mu / ms) * (mu / ms) - 0.5 * log(2 * M_PI) - log(ms);
   lp += -log(M_PI) - log(ts) - log1p((tau / ts) * (tau / ts)) + log(2.0) + lt;
   double sw = 0, swe = 0;
   for (int j = 0; j < J; ++j) {
-    double eta = z[2 + j], s = m->sigma[j], th = mu + tau * eta, r = (m->y[j] - th) / s;
+    double eta = z[2 + j], s = ss[j], th = mu + tau * eta, r = (ys[j] - th) / s;
     lp += -0.5 * eta * eta - 0.5 * r * r - log(s) - log(2 * M_PI);
     double w = r / s;
     sw += w;
@@ -147,13 +201,148 @@ static double hier_pg(const model_t* m, const real* z, real* g) {
   return -lp;
 }
 
-static double potential_grad(const model_t* m, const real* z, real* g) {
-  return m->family == 2 ? logreg_pg(m, z, g) : hier_pg(m, z, g);
+/* Horseshoe regression (potentials_ref.horseshoe_* / horseshoe_nc_*), FP64 arithmetic.
+ * centred:     z = [beta(P), log lambda(P), log sigma, log tau]
+ * non-centred: z = [log lambda(P), log sigma, log tau, unscaled_betas(P)], beta = tau lambda eta */
+static double horseshoe_pg(const nutsref_model* m, const real* z, real* g) {
+  const int P = m->P;
+  const int64_t N = m->N;
+  const int nc = m->hyper[0] != 0.0;
+  const real* llam = nc ? z : z + P;
+  const double lsig = nc ? z[P] : z[2 * P], ltau = nc ? z[P + 1] : z[2 * P + 1];
+  const double sig = exp(lsig), tau = exp(ltau);
+  double* beta = (double*)malloc(sizeof(double) * (size_t)P);
+  double* gx = (double*)calloc((size_t)P, sizeof(double));
+  for (int d = 0; d < P; ++d) beta[d] = nc ? tau * exp((double)llam[d]) * (double)z[P + 2 + d] : (double)z[d];
+  double rr = 0.0;
+  for (int64_t n = 0; n < N; ++n) {
+    const float* x = m->X + n * P;
+    double acc = 0.0;
+#pragma omp simd reduction(+ : acc)
+    for (int d = 0; d < P; ++d) acc += (double)x[d] * beta[d];
+    const double r = (double)m->y[n] - acc;
+    rr += r * r;
+    for (int d = 0; d < P; ++d) gx[d] += r * (double)x[d];
+  }
+  const double inv_s2 = 1.0 / (sig * sig);
+  for (int d = 0; d < P; ++d) gx[d] *= inv_s2; /* -dU_lik/dbeta */
+  double lp = 0.0;
+  /* likelihood: Normal(resid; 0, sigma) */
+  lp += -0.5 * rr * inv_s2 - (double)N * (0.5 * LOG_2PI + lsig);
+  /* sigma ~ HalfNormal(1) with its Exp log-det */
+  lp += -0.5 * sig * sig - 0.5 * LOG_2PI + LOG_2 + lsig;
+  /* tau ~ HalfCauchy(1) */
+  lp += -LOG_PI - log1p(tau * tau) + LOG_2 + ltau;
+  double gtau = 0.0;
+  for (int d = 0; d < P; ++d) {
+    const double ll = llam[d], lam = exp(ll);
+    lp += -LOG_PI - log1p(lam * lam) + LOG_2 + ll; /* lambda_d ~ HalfCauchy(1) */
+    if (nc) {
+      const double eta = z[P + 2 + d];
+      lp += -0.5 * eta * eta - 0.5 * LOG_2PI;
+      g[P + 2 + d] = (real)(eta - tau * lam * gx[d]);
+      g[d] = (real)(-beta[d] * gx[d] + 2.0 * lam * lam / (1.0 + lam * lam) - 1.0);
+      gtau += -beta[d] * gx[d];
+    } else {
+      const double s = tau * lam, b = beta[d], q = b * b / (s * s);
+      lp += -0.5 * q - 0.5 * LOG_2PI - log(s);
+      g[d] = (real)(b / (s * s) - gx[d]);
+      g[P + d] = (real)(-q + 2.0 * lam * lam / (1.0 + lam * lam));
+      gtau += -q + 1.0;
+    }
+  }
+  const int is = nc ? P : 2 * P;
+  g[is] = (real)(sig * sig - 1.0 - rr * inv_s2 + (double)N);
+  g[is + 1] = (real)(gtau + 2.0 * tau * tau / (1.0 + tau * tau) - 1.0);
+  free(beta);
+  free(gx);
+  return -lp;
+}
+
+/* Stochastic volatility (potentials_ref.sv_* / sv_nc_*), FP64 arithmetic.
+ * centred:     z = [h(T), log nu, log s], h ~ GaussianRandomWalk(s)
+ * non-centred: z = [h_base(T), log nu, log s], h = s cumsum(h_base) */
+static double sv_pg(const nutsref_model* m, const real* z, real* g) {
+  const int T = (int)m->N;
+  const double s_rate = m->hyper[0] > 0 ? m->hyper[0] : 10.0, nu_rate = m->hyper[1] > 0 ? m->hyper[1] : 0.1;
+  const int nc = m->hyper[2] != 0.0;
+  const double lnu = z[T], ls = z[T + 1], nu = exp(lnu), s = exp(ls);
+  double lp = log(s_rate) - s_rate * s + ls + log(nu_rate) - nu_rate * nu + lnu;
+  const double zc = 0.5 * lnu + 0.5 * LOG_PI + lgamma(0.5 * nu) - lgamma(0.5 * (nu + 1.0));
+  const double dig = -0.5 / nu - 0.5 * digamma_ref(0.5 * nu) + 0.5 * digamma_ref(0.5 * (nu + 1.0));
+  double dlp_dnu = 0.0, sumsq = 0.0, as = 0.0, cum = 0.0;
+  double* a = (double*)malloc(sizeof(double) * (size_t)T);
+  double* S = (double*)malloc(sizeof(double) * (size_t)T);
+  for (int t = 0; t < T; ++t) {
+    double h;
+    if (nc) {
+      cum += (double)z[t];
+      S[t] = cum;
+      h = s * cum;
+      lp += -0.5 * (double)z[t] * (double)z[t] - 0.5 * LOG_2PI;
+    } else {
+      h = z[t];
+      const double d = t == 0 ? (double)z[0] : (double)z[t] - (double)z[t - 1];
+      sumsq += d * d;
+    }
+    const double yv = (double)m->y[t] * exp(-h), y2 = yv * yv;
+    lp += -0.5 * (nu + 1.0) * log1p(y2 / nu) - (h + zc);
+    a[t] = (nu + 1.0) * y2 / (nu + y2) - 1.0; /* d log StudentT / d h_t */
+    dlp_dnu += -0.5 * log1p(y2 / nu) + 0.5 * (nu + 1.0) * y2 / (nu * (nu + y2)) + dig;
+  }
+  if (!nc) lp += -0.5 * sumsq / (s * s) - (double)T * (0.5 * LOG_2PI + ls);
+  dlp_dnu += -nu_rate;
+  g[T] = (real)(-(dlp_dnu * nu + 1.0));
+  if (nc) {
+    double suffix = 0.0;
+    for (int t = T - 1; t >= 0; --t) {
+      suffix += a[t];
+      g[t] = (real)((double)z[t] - s * suffix);
+      as += a[t] * S[t];
+    }
+    g[T + 1] = (real)(-s * as + s_rate * s - 1.0);
+  } else {
+    const double is2 = 1.0 / (s * s);
+    for (int t = 0; t < T; ++t) {
+      double gh = 0.0;
+      const double dprev = t == 0 ? (double)z[0] : (double)z[t] - (double)z[t - 1];
+      gh += dprev * is2;
+      if (t + 1 < T) gh -= ((double)z[t + 1] - (double)z[t]) * is2;
+      g[t] = (real)(gh - a[t]);
+    }
+    const double dlp_ds = sumsq / (s * s * s) - (double)T / s - s_rate;
+    g[T + 1] = (real)(-(dlp_ds * s + 1.0));
+  }
+  free(a);
+  free(S);
+  return -lp;
+}
+
+static double potential_grad(const nutsref_model* m, int k, const real* z, real* g) {
+  switch (m->family) {
+    case 1: return hier_pg(m, k, z, g);
+    case 2: return logreg_pg(m, z, g);
+    case 3: return horseshoe_pg(m, z, g);
+    default: return sv_pg(m, z, g);
+  }
+}
+
+/* U and dU/dz of one latent point of dataset model_index (FP64 in and out). */
+double nutsref_potential(const nutsref_model* m, int model_index, const double* z, double* g) {
+  int D = nutsref_latent_dim(m, model_index);
+  real* zr = (real*)malloc(sizeof(real) * (size_t)D);
+  real* gr = (real*)malloc(sizeof(real) * (size_t)D);
+  for (int d = 0; d < D; ++d) zr[d] = (real)z[d];
+  double pe = potential_grad(m, model_index, zr, gr);
+  for (int d = 0; d < D; ++d) g[d] = (double)gr[d];
+  free(zr);
+  free(gr);
+  return pe;
 }
 
 /* ------------------------------------------------------------------ chain */
 typedef struct {
-  int D, maxd;
+  int D, maxd, k; /* latent dim, checkpoint rows, dataset index */
   real *z, *g, *inv, *msq;
   real *zl, *rl, *gl, *zr, *rr, *gr, *zp, *gp, *zsp, *gsp, *rs, *rss, *rck, *sck, *tmp;
   double pe, step, ss[5];
@@ -161,6 +350,26 @@ typedef struct {
   int mm_n, window_idx;
   long grad_evals;
 } chain_t;
+
+static void chain_alloc(chain_t* c, int D, int maxd, int k) {
+  c->D = D;
+  c->maxd = maxd;
+  c->k = k;
+  real** vs[] = {&c->z, &c->g, &c->inv, &c->msq, &c->zl, &c->rl, &c->gl, &c->zr, &c->rr, &c->gr, &c->zp,
+                 &c->gp, &c->zsp, &c->gsp, &c->rs, &c->rss, &c->tmp};
+  for (size_t v = 0; v < sizeof(vs) / sizeof(vs[0]); ++v) *vs[v] = (real*)calloc((size_t)D, sizeof(real));
+  c->rck = (real*)calloc((size_t)maxd * D, sizeof(real));
+  c->sck = (real*)calloc((size_t)maxd * D, sizeof(real));
+  c->mean = (double*)calloc((size_t)D, sizeof(double));
+  c->m2 = (double*)calloc((size_t)D, sizeof(double));
+}
+
+static void chain_free(chain_t* c) {
+  real** vs[] = {&c->z, &c->g, &c->inv, &c->msq, &c->zl, &c->rl, &c->gl, &c->zr, &c->rr, &c->gr, &c->zp,
+                 &c->gp, &c->zsp, &c->gsp, &c->rs, &c->rss, &c->tmp};
+  for (size_t v = 0; v < sizeof(vs) / sizeof(vs[0]); ++v) free(*vs[v]);
+  free(c->rck); free(c->sck); free(c->mean); free(c->m2);
+}
 
 static double kinetic(const chain_t* c, const real* r) {
   double k = 0;
@@ -188,19 +397,19 @@ static double logaddexp(double a, double b) {
 }
 
 /* one leapfrog from the frontier (z, r, g) in place; returns pe */
-static double leapfrog(const model_t* m, chain_t* c, real* z, real* r, real* g, double eps) {
+static double leapfrog(const nutsref_model* m, chain_t* c, real* z, real* r, real* g, double eps) {
   for (int d = 0; d < c->D; ++d) {
     r[d] = (real)((double)r[d] - 0.5 * eps * g[d]);
     z[d] = (real)((double)z[d] + eps * (double)c->inv[d] * r[d]);
   }
-  double pe = potential_grad(m, z, g);
+  double pe = potential_grad(m, c->k, z, g);
   c->grad_evals++;
   for (int d = 0; d < c->D; ++d) r[d] = (real)((double)r[d] - 0.5 * eps * g[d]);
   return pe;
 }
 
 /* One NUTS transition (hmc.py:459-530 with build_tree hmc_util.py:1088-1180). */
-static void nuts_transition(const model_t* m, chain_t* c, seed_t s, uint32_t chain, uint32_t n, int max_depth,
+static void nuts_transition(const nutsref_model* m, chain_t* c, seed_t s, uint32_t chain, uint32_t n, int max_depth,
                             int* num_steps, double* accept_prob, int* diverging) {
   int D = c->D;
   real* r0 = c->tmp;
@@ -338,18 +547,61 @@ static double now_s(void) {
 }
 
 /*
- * Runs `chains` independent chains (ids first_chain..) for num_warmup +
- * num_samples NUTS transitions.  If init_z is given ([chains][D], with
- * init_step/init_inv), warmup adaptation is skipped and num_warmup
- * transitions run without adaptation.  samples: [chains][num_samples][D].
+ * Replays one NUTS transition for each of `chains` chains from a given state, without
+ * adaptation: chain k has global id chain_ids[k] (its Philox stream and, for the
+ * hierarchical family, its dataset), transition counter iters[k], position z0 (row k of a
+ * [chains][ld] array), step size step[k], and diagonal mass rows inv / msq ([chains][ld];
+ * msq = mass_matrix_sqrt).  The potential at z0 is recomputed here.  Outputs: z_out
+ * [chains][ld], num_steps, accept_prob, diverging, potential energy of the new state.
+ */
+int nutsref_transitions(const nutsref_model* m, int chains, const uint32_t* chain_ids, const uint32_t* iters, int ld,
+                        const float* z0, const float* step, const float* inv, const float* msq, uint64_t seed,
+                        int max_depth, int threads, float* z_out, int32_t* num_steps, double* accept_prob,
+                        uint8_t* diverging, double* pe_out) {
+  seed_t s = {(uint32_t)(seed & 0xffffffffu), (uint32_t)(seed >> 32)};
+#ifdef _OPENMP
+  if (threads > 0) omp_set_num_threads(threads);
+#endif
+#pragma omp parallel for schedule(dynamic, 1)
+  for (int k = 0; k < chains; ++k) {
+    chain_t c;
+    memset(&c, 0, sizeof(c));
+    const int mk = model_of_chain(m, chain_ids[k]);
+    const int D = nutsref_latent_dim(m, mk);
+    chain_alloc(&c, D, max_depth, mk);
+    for (int d = 0; d < D; ++d) {
+      c.z[d] = (real)z0[(size_t)k * ld + d];
+      c.inv[d] = (real)inv[(size_t)k * ld + d];
+      c.msq[d] = (real)msq[(size_t)k * ld + d];
+    }
+    c.step = (real)step[k];
+    c.pe = potential_grad(m, mk, c.z, c.g);
+    int ns = 0, dv = 0;
+    double ap = 0.0;
+    nuts_transition(m, &c, s, chain_ids[k], iters[k], max_depth, &ns, &ap, &dv);
+    for (int d = 0; d < ld; ++d) z_out[(size_t)k * ld + d] = d < D ? (float)c.z[d] : 0.0f;
+    num_steps[k] = ns;
+    accept_prob[k] = ap;
+    diverging[k] = (uint8_t)dv;
+    pe_out[k] = c.pe;
+    chain_free(&c);
+  }
+  return 0;
+}
+
+/*
+ * Runs `chains` independent chains (ids first_chain..) for num_warmup + num_samples NUTS
+ * transitions of model m.  If init_z is given ([chains][ld], with init_step/init_inv),
+ * warmup adaptation is skipped and num_warmup transitions run without adaptation; else
+ * init_to_uniform(radius=2) and the Stan warmup (dual averaging, diagonal Welford).
+ * samples: [chains][num_samples][ld]; num_steps_out / diverging_out: [chains][num_samples];
+ * adapted_step [chains] and adapted_inv [chains][ld] receive the state after warmup (may be NULL).
  * timing: [warmup_s, sampling_s, warmup_grad_evals, sampling_grad_evals, threads].
  */
-int nutsref_run(int family, const float* X, const float* y, const float* sigma, int64_t N, int D, double h0,
-                double h1, int chains, int first_chain, int num_warmup, int num_samples, uint64_t seed,
-                int max_tree_depth, int threads, const float* init_z, const float* init_step,
-                const float* init_inv, float* samples, int32_t* num_steps_out, double* timing,
-                double warmup_budget_s) {
-  model_t m = {family, N, D, X, y, sigma, {h0, h1, 0, 0}};
+int nutsref_run_model(const nutsref_model* m, int ld, int chains, int first_chain, int num_warmup, int num_samples,
+                      uint64_t seed, int max_tree_depth, int threads, const float* init_z, const float* init_step,
+                      const float* init_inv, float* samples, int32_t* num_steps_out, uint8_t* diverging_out,
+                      float* adapted_step, float* adapted_inv, double* timing, double warmup_budget_s) {
   seed_t s = {(uint32_t)(seed & 0xffffffffu), (uint32_t)(seed >> 32)};
   int ends[64];
   int nwin = window_ends(num_warmup, ends);
@@ -362,20 +614,14 @@ int nutsref_run(int family, const float* X, const float* y, const float* sigma, 
   int maxd = max_tree_depth;
   for (int k = 0; k < chains; ++k) {
     chain_t* c = &cs[k];
-    c->D = D;
-    c->maxd = maxd;
-    real** vs[] = {&c->z, &c->g, &c->inv, &c->msq, &c->zl, &c->rl, &c->gl, &c->zr, &c->rr, &c->gr, &c->zp,
-                   &c->gp, &c->zsp, &c->gsp, &c->rs, &c->rss, &c->tmp};
-    for (size_t v = 0; v < sizeof(vs) / sizeof(vs[0]); ++v) *vs[v] = (real*)calloc((size_t)D, sizeof(real));
-    c->rck = (real*)calloc((size_t)maxd * D, sizeof(real));
-    c->sck = (real*)calloc((size_t)maxd * D, sizeof(real));
-    c->mean = (double*)calloc((size_t)D, sizeof(double));
-    c->m2 = (double*)calloc((size_t)D, sizeof(double));
     uint32_t chain = (uint32_t)(first_chain + k);
+    const int mk = model_of_chain(m, chain);
+    const int D = nutsref_latent_dim(m, mk);
+    chain_alloc(c, D, maxd, mk);
     if (init_z) {
       for (int d = 0; d < D; ++d) {
-        c->z[d] = init_z[(size_t)k * D + d];
-        c->inv[d] = init_inv[(size_t)k * D + d];
+        c->z[d] = init_z[(size_t)k * ld + d];
+        c->inv[d] = init_inv[(size_t)k * ld + d];
         c->msq[d] = (real)(1.0 / sqrt((double)c->inv[d]));
       }
       c->step = init_step[k];
@@ -394,14 +640,14 @@ int nutsref_run(int family, const float* X, const float* y, const float* sigma, 
 #pragma omp parallel for schedule(dynamic, 1) reduction(+ : gw)
   for (int k = 0; k < chains; ++k) {
     chain_t* c = &cs[k];
-    c->pe = potential_grad(&m, c->z, c->g);
+    c->pe = potential_grad(m, c->k, c->z, c->g);
     uint32_t chain = (uint32_t)(first_chain + k);
     for (int t = 0; t < num_warmup; ++t) {
       int ns, dv;
       double ap;
       /* a bounded baseline may cut the warmup short; it is reported as such */
       if (warmup_budget_s > 0 && now_s() - tw0 > warmup_budget_s) break;
-      nuts_transition(&m, c, s, chain, (uint32_t)t, max_tree_depth, &ns, &ap, &dv);
+      nuts_transition(m, c, s, chain, (uint32_t)t, max_tree_depth, &ns, &ap, &dv);
       if (!init_z) adapt(c, t, ap, num_warmup, ends, nwin);
     }
     gw += c->grad_evals;
@@ -412,12 +658,17 @@ int nutsref_run(int family, const float* X, const float* y, const float* sigma, 
   for (int k = 0; k < chains; ++k) {
     chain_t* c = &cs[k];
     uint32_t chain = (uint32_t)(first_chain + k);
+    if (adapted_step) adapted_step[k] = (float)c->step;
+    if (adapted_inv)
+      for (int d = 0; d < ld; ++d) adapted_inv[(size_t)k * ld + d] = d < c->D ? (float)c->inv[d] : 0.0f;
     for (int t = 0; t < num_samples; ++t) {
       int ns, dv;
       double ap;
-      nuts_transition(&m, c, s, chain, (uint32_t)(num_warmup + t), max_tree_depth, &ns, &ap, &dv);
-      for (int d = 0; d < D; ++d) samples[((size_t)k * num_samples + t) * D + d] = (float)c->z[d];
+      nuts_transition(m, c, s, chain, (uint32_t)(num_warmup + t), max_tree_depth, &ns, &ap, &dv);
+      for (int d = 0; d < ld; ++d)
+        samples[((size_t)k * num_samples + t) * ld + d] = d < c->D ? (float)c->z[d] : 0.0f;
       if (num_steps_out) num_steps_out[(size_t)k * num_samples + t] = ns;
+      if (diverging_out) diverging_out[(size_t)k * num_samples + t] = (uint8_t)dv;
     }
     gs += c->grad_evals;
   }
@@ -431,16 +682,32 @@ int nutsref_run(int family, const float* X, const float* y, const float* sigma, 
   timing[2] = (double)gw;
   timing[3] = (double)gs;
   timing[4] = (double)nthreads;
-  if (init_z == NULL && init_step) {
-    /* return the adapted state through the init pointers' shapes is not supported */
-  }
-  for (int k = 0; k < chains; ++k) {
-    chain_t* c = &cs[k];
-    real** vs[] = {&c->z, &c->g, &c->inv, &c->msq, &c->zl, &c->rl, &c->gl, &c->zr, &c->rr, &c->gr, &c->zp,
-                   &c->gp, &c->zsp, &c->gsp, &c->rs, &c->rss, &c->tmp};
-    for (size_t v = 0; v < sizeof(vs) / sizeof(vs[0]); ++v) free(*vs[v]);
-    free(c->rck); free(c->sck); free(c->mean); free(c->m2);
-  }
+  for (int k = 0; k < chains; ++k) chain_free(&cs[k]);
   free(cs);
   return 0;
+}
+
+/* The logistic / eight-schools entry point of the CPU baseline (family 1 with one dataset of
+ * N groups, or family 2 with P = D features); see nutsref_run_model. */
+int nutsref_run(int family, const float* X, const float* y, const float* sigma, int64_t N, int D, double h0,
+                double h1, int chains, int first_chain, int num_warmup, int num_samples, uint64_t seed,
+                int max_tree_depth, int threads, const float* init_z, const float* init_step,
+                const float* init_inv, float* samples, int32_t* num_steps_out, double* timing,
+                double warmup_budget_s) {
+  nutsref_model m;
+  memset(&m, 0, sizeof(m));
+  m.family = family;
+  m.num_models = 1;
+  m.chains_per_model = chains + first_chain;
+  m.P = family == 2 ? D : 0;
+  m.N = N;
+  m.X = X;
+  m.y = y;
+  m.sigma = sigma;
+  m.offsets = NULL;
+  m.hyper[0] = h0;
+  m.hyper[1] = h1;
+  return nutsref_run_model(&m, D, chains, first_chain, num_warmup, num_samples, seed, max_tree_depth, threads,
+                           init_z, init_step, init_inv, samples, num_steps_out, NULL, NULL, NULL, timing,
+                           warmup_budget_s);
 }

@@ -63,3 +63,59 @@ def typical_points(name, model, rng, C):
         z[:, 2 * P + 1] = -2.0 + 0.3 * rng.standard_normal(C)
         return z.astype(np.float32)
     return rng.uniform(-2, 2, (C, D)).astype(np.float32)
+
+
+def replay_parity(kernel, state, cmodel, seed, transitions, max_tree_depth=10, threads=0):
+    """Runs ``transitions`` GPU transitions of ``kernel`` from ``state`` (after warmup, so
+    without adaptation) and replays each one with the FP64 C oracle from the GPU's own
+    starting state (position, step size, mass rows) at the same Philox stream addresses.
+    Returns counts of identical tree sizes / divergence flags and the relative position
+    errors of the transitions whose tree sizes agree."""
+    from oracle import build_oracle as B
+
+    lib = B.load("f64")
+    same, total, zerr, aperr, st = 0, 0, [], [], state
+    for _ in range(transitions):
+        z0 = st.z.cpu().numpy()
+        step = st.adapt_state.step_size.cpu().numpy()
+        inv = st.adapt_state.inverse_mass_matrix.cpu().numpy()
+        msq = st.adapt_state.mass_matrix_sqrt.cpu().numpy()
+        key = st.rng_key.cpu().numpy().astype(np.uint32)
+        new = kernel.sample(st)
+        ns = new.num_steps.cpu().numpy()
+        dv = new.diverging.cpu().numpy().astype(bool)
+        zg = new.z.cpu().numpy()
+        ap = new.accept_prob.cpu().numpy()
+        ref = B.transitions(lib, cmodel, z0, step, inv, msq, key[:, 0], key[:, 1], seed,
+                            max_tree_depth=max_tree_depth, threads=threads)
+        for c in range(z0.shape[0]):
+            total += 1
+            if ref["num_steps"][c] == ns[c] and ref["diverging"][c] == dv[c]:
+                same += 1
+                aperr.append(abs(ref["accept_prob"][c] - ap[c]))
+                rz = ref["z"][c].astype(np.float64)
+                zerr.append(np.max(np.abs(rz - zg[c]) / (np.abs(rz) + 1e-2)))
+        st = new
+    return {"same": same, "total": total, "frac": same / total, "zerr": np.array(zerr), "aperr": np.array(aperr),
+            "state": st}
+
+
+def cmodel_of(model, chains_per_model=1):
+    """The C oracle's copy of a registry model (oracle/nuts_ref.c nutsref_model)."""
+    from oracle import build_oracle as B
+
+    if isinstance(model, models.HierarchicalNormal):
+        y = np.concatenate([a for a, _ in model.datasets])
+        s = np.concatenate([b for _, b in model.datasets])
+        off = np.zeros(model.num_models + 1, np.int32)
+        off[1:] = np.cumsum(model.J)
+        return B.Model("hier_nc", y=y, sigma=s, offsets=off, chains_per_model=chains_per_model,
+                       hyper=(model.mu_scale, model.tau_scale))
+    if isinstance(model, models.LogisticRegression):
+        return B.Model("logreg", X=model.X, y=model.y, hyper=(model.prior_scale,))
+    if isinstance(model, models.HorseshoeRegression):
+        return B.Model("horseshoe_nc" if model.noncentered else "horseshoe", X=model.X, y=model.y)
+    if isinstance(model, models.StochasticVolatility):
+        return B.Model("sv_nc" if model.noncentered else "sv", y=model.returns,
+                       hyper=(model.s_rate, model.nu_rate, 1.0 if model.noncentered else 0.0))
+    raise TypeError(model)
