@@ -53,17 +53,22 @@ def parse():
                    choices=["logreg", "eight_schools", "uneven_hier", "horseshoe", "horseshoe_nc", "sv", "sv_nc"],
                    help="non-default workloads: a full warmup+sampling run of that model family")
     p.add_argument("--samples", type=int, default=None, help="sampling iterations of a --workload run")
+    p.add_argument("--full-samples", type=int, default=1000,
+                   help="sampling iterations of the full run (500 warmup + this) reported beside the timed steps")
+    p.add_argument("--oracle-samples", type=int, default=30,
+                   help="transitions per chain of the FP64 oracle leg of the posterior check; 0 = skip")
+    p.add_argument("--no-workloads", action="store_true",
+                   help="skip the other benchmark configurations (eight schools, uneven hierarchical, horseshoe, SV)")
     return p.parse_args()
 
 
-def run_workload(args):
-    """Full NUTS run (warmup + sampling, both timed with CUDA events) of one of the
-    other model families at its benchmark shape; prints one JSON line."""
+def workload_run(w, precision=None, num_warmup=None, num_samples=None):
+    """Full NUTS run (warmup + sampling, both timed with CUDA events) of one of the other
+    benchmark configurations at its shape; returns the figures of one JSON sub-object."""
     import torch
 
     from numpyro_gb300 import NUTS, datasets, models
 
-    w = args.workload
     if w == "eight_schools":
         y, s = datasets.eight_schools(0)
         model, C, W, S = models.HierarchicalNormal(y, s), 4, 1000, 1000
@@ -84,14 +89,14 @@ def run_workload(args):
         nc = w == "sv_nc"
         model, C, W, S = models.StochasticVolatility(r, noncentered=nc), 256, 1000, 1000
         shape = "T=4096 (D=4098), 256 chains, %s walk" % ("non-centred" if nc else "centred")
-    if args.num_warmup != 500:
-        W = args.num_warmup
-    if args.samples:
-        S = args.samples
-    kw = {"precision": args.precision} if args.precision else {}
+    if num_warmup is not None:
+        W = num_warmup
+    if num_samples:
+        S = num_samples
+    kw = {"precision": precision} if precision else {}
     k = NUTS(model, num_chains=C, **kw)
-    if args.precision:
-        shape += ", precision " + args.precision
+    if precision:
+        shape += ", precision " + precision
     log("%s: %s, %d warmup + %d samples" % (w, shape, W, S))
     st = k.init(1, W)
     ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
@@ -105,6 +110,7 @@ def run_workload(args):
     warm_s, samp_s = ev[0].elapsed_time(ev[1]) / 1e3, ev[1].elapsed_time(ev[2]) / 1e3
     ticks = k.stats()["ticks"] - t_ticks
     ns = out["num_steps"].cpu().numpy()
+    divergences = int(out["diverging"].sum().item())
     if w in ("sv", "sv_nc"):
         # every 16th step of the walk plus nu and s keeps the host-side ranking to ~260 coordinates;
         # the non-centred run adds the derived walk h = s * cumsum(h_base) at the same steps
@@ -124,6 +130,7 @@ def run_workload(args):
         z = out["z"].index_select(0, rows).cpu().numpy()
     else:
         z = out["z"].cpu().numpy()
+    del out
     if w == "uneven_hier":  # ESS per model over its 4 chains, padding excluded
         ess, rhat = [], []
         for i, m in enumerate(picked):
@@ -138,15 +145,45 @@ def run_workload(args):
     else:
         ess_min, rhat_max = min_bulk_ess(z)
         ess_note = "min over latent coordinates"
+    grad_evals = float(ns.sum())
+    burst, _, hbm, peak_kind = measured_peaks()
+    if w == "eight_schools":
+        # 4 chains: a latency figure, the time of one leapfrog step of one chain
+        roof = {"bound": "latency", "us_per_leapfrog_step": 1e6 * samp_s / (grad_evals / C)}
+    elif w == "uneven_hier":
+        # 24 D_c bytes of chain state (z, r, grad read and written) + 8 J_c bytes of data per evaluation
+        J = np.array([model.chain_latent_dim(c, 4) - 2 for c in range(C)], np.float64)
+        nbytes = float(np.sum(ns.sum(axis=1) * (24.0 * (J + 2) + 8.0 * J)))
+        gbs = nbytes / samp_s / 1e9
+        roof = {"bound": "hbm", "achieved": gbs, "peak": hbm, "unit": "GB/s", "frac": gbs / hbm,
+                "bytes_per_grad_eval": "24 (J_c + 2) + 8 J_c", "peak_kind": peak_kind}
+    elif w in ("sv", "sv_nc"):
+        T = model.latent_dim - 2
+        per = 24.0 * (T + 2) + 4.0 * T
+        gbs = grad_evals * per / samp_s / 1e9
+        roof = {"bound": "hbm", "achieved": gbs, "peak": hbm, "unit": "GB/s", "frac": gbs / hbm,
+                "bytes_per_grad_eval": per, "peak_kind": peak_kind}
+    else:
+        N, P = 2000, 1000
+        tf = grad_evals * 4.0 * N * P / samp_s / 1e12
+        roof = {"bound": "tensor" if precision == "bf16x3" else "fp32", "achieved": tf, "peak": burst,
+                "unit": "TFLOP/s", "frac": tf / burst, "flop_per_grad_eval": 4.0 * N * P,
+                "peak_kind": peak_kind + " burst bf16"}
     line = {"workload": w, "shape": shape, "chains": C, "num_warmup": W, "num_samples": S,
-            "warmup_s": warm_s, "sampling_s": samp_s, "grad_evals_per_s_sampling": float(ns.sum()) / samp_s,
-            "mean_num_steps": float(ns.mean()), "divergences": int(out["diverging"].sum().item()),
+            "warmup_s": warm_s, "sampling_s": samp_s, "grad_evals_per_s_sampling": grad_evals / samp_s,
+            "mean_num_steps": float(ns.mean()), "divergences": divergences,
             "min_bulk_ess": ess_min, "min_bulk_ess_per_s_sampling": ess_min / samp_s,
             "min_bulk_ess_per_s_total": ess_min / (warm_s + samp_s), "rhat_max": rhat_max,
             "ess_definition": ess_note, "ticks_sampling": ticks, "us_per_tick": 1e6 * samp_s / max(1, ticks),
-            "tuning": k.tuning()}
-    print(json.dumps(line))
+            "roofline": roof, "tuning": k.tuning()}
     k.close()
+    return line
+
+
+def run_workload(args):
+    """--workload: one JSON line for one of the other benchmark configurations."""
+    print(json.dumps(workload_run(args.workload, args.precision,
+                                  None if args.num_warmup == 500 else args.num_warmup, args.samples)))
     return 0
 
 
@@ -284,25 +321,88 @@ def cpu_baseline(X, y, chains, num_samples, init=None, num_warmup=0, budget_s=0.
     }
 
 
+def oracle_moment_check(X, y, state, zgpu, chains, transitions):
+    """The GPU posterior against the FP64 oracle's: the C oracle (FP64 build) runs ``chains``
+    chains for ``transitions`` NUTS transitions from the GPU's adapted state, and each
+    coefficient's posterior mean and sd are compared, in units of their Monte Carlo standard
+    error (sd / sqrt(bulk-ESS), combined over both samples; for the sd, sd / sqrt(2 ESS))."""
+    from oracle import build_oracle
+    from numpyro_gb300.diagnostics import bulk_effective_sample_size
+
+    lib = build_oracle.load("f64")
+    cores = len(os.sched_getaffinity(0))
+    init = (state.z[:chains].cpu().numpy(), state.adapt_state.step_size[:chains].cpu().numpy(),
+            state.adapt_state.inverse_mass_matrix[:chains].cpu().numpy())
+    # the oracle chains start where the GPU chains stood; they continue from there on their own stream
+    res = build_oracle.run_logreg(lib, X, y, chains=chains, num_warmup=0, num_samples=transitions, seed=7,
+                                  threads=min(cores, chains), init=init, first_chain=0)
+    zo = np.asarray(res["samples"], np.float64)
+    zg = np.asarray(zgpu, np.float64)
+
+    def moments(z):
+        m = z.mean(axis=(0, 1))
+        sd = z.std(axis=(0, 1), ddof=1)
+        ess = np.concatenate([np.atleast_1d(bulk_effective_sample_size(z[..., d0:d0 + 64]))
+                              for d0 in range(0, z.shape[-1], 64)])
+        return m, sd, ess
+
+    mg, sg, eg = moments(zg)
+    mo, so, eo = moments(zo)
+    mcse_m = np.sqrt(sg ** 2 / eg + so ** 2 / eo)
+    mcse_s = np.sqrt(sg ** 2 / (2 * eg) + so ** 2 / (2 * eo))
+    zm = np.abs(mg - mo) / mcse_m
+    zs = np.abs(sg - so) / mcse_s
+    return {"oracle": "FP64 C restatement of numpyro's NUTS, %d chains x %d transitions from the GPU's "
+                      "adapted state (%.0f s on %d host threads)" % (chains, transitions, res["sampling_s"],
+                                                                    res["threads"]),
+            "gpu_draws": "%d chains x %d draws" % zg.shape[:2],
+            "max_abs_dmean_over_mcse": float(zm.max()), "max_abs_dsd_over_mcse": float(zs.max()),
+            "coords_beyond_3_mcse": int(np.sum(zm > 3) + np.sum(zs > 3)), "coords": int(zg.shape[-1]),
+            "oracle_min_bulk_ess": float(eo.min())}
+
+
 def run_reference(args):
     """--impl reference: numpyro itself cannot run here (no jax); its NUTS algorithm runs as the
-    C oracle port on the host cores: a bounded Stan warmup, then --steps sampling steps."""
+    C restatement (FP32 build, numpyro's default dtype) on the host cores, on the workload of our
+    arm: the same 500-iteration Stan warmup from init_to_uniform, then --steps sampling steps of
+    --iters-per-step transitions.  A bounded sample of the 1024 chains: 4 chains, each evaluating
+    its potential on all host threads (rows split across the threads, as XLA's CPU backend splits
+    one chain's matrix products), run one after another."""
     from numpyro_gb300 import datasets
+    from oracle import build_oracle
 
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return 0
     X, y, _ = datasets.covtype_like(seed=0, n=args.n)
-    chains = min(16, len(os.sched_getaffinity(0)))
-    per_step = 5
-    cb = cpu_baseline(X, y, chains=chains, num_samples=max(4, args.steps * per_step), num_warmup=100,
-                      budget_s=150.0)
-    line = {"metric": METRIC, "value": cb["value"], "unit": "ESS/s", "impl": "reference", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * cb["sampling_s"] / max(1, args.steps),
+    cores = len(os.sched_getaffinity(0))
+    chains = 4
+    B = args.iters_per_step
+    S = max(4, args.steps * B)
+    lib = build_oracle.load("f32")
+    model = build_oracle.Model("logreg", X=X, y=y, row_threads=cores)
+    budget_s = 300.0
+    res = build_oracle.run_model(lib, model, X.shape[1], chains, args.num_warmup, S, seed=0, threads=cores,
+                                 warmup_budget_s=budget_s)
+    ess, rhat = min_bulk_ess(res["samples"])
+    value = ess / res["sampling_s"]
+    sample = ("%d of the 1024 chains: init_to_uniform, %d-iteration Stan warmup (%.0f s, %s), then %d sampling "
+              "transitions each (max_tree_depth 10) on the full N=%d x %d data; FP32 C restatement of numpyro's "
+              "NUTS with each chain's potential split across %d host threads; ESS/s = min bulk-ESS of the sampling "
+              "draws / sampling seconds" % (chains, args.num_warmup, res["warmup_s"],
+                                            "completed" if res["warmup_s"] < budget_s else "cut at the time budget",
+                                            S, X.shape[0], X.shape[1], cores))
+    cb = {"value": value, "unit": "ESS/s", "cores": cores, "kind": "port", "sample": sample,
+          "grad_evals_per_s": res["sampling_grad_evals"] / res["sampling_s"], "sampling_s": res["sampling_s"],
+          "warmup_s": res["warmup_s"], "warmup_grad_evals": res["warmup_grad_evals"], "min_bulk_ess": ess,
+          "rhat_max": rhat}
+    line = {"metric": METRIC, "value": value, "unit": "ESS/s", "impl": "reference", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * res["sampling_s"] / max(1, args.steps),
             "higher_is_better": True, "scaling": "weak", "dtype": "f32", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "chains_timed": chains, "iters_per_step": per_step},
+            "config": {"workload": WORKLOAD, "chains_timed": chains, "iters_per_step": B,
+                       "num_warmup": args.num_warmup},
             "cpu_baseline": cb,
-            "e2e": {"value": cb["value"], "unit": "ESS/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "e2e": {"value": value, "unit": "ESS/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "grad_evals_per_s": cb["grad_evals_per_s"], "vs_baseline": None}
     print(json.dumps(line))
     return 0
@@ -404,13 +504,16 @@ def main():
     burst, sustained, hbm, peak_kind = measured_peaks()
     flop = 4.0 * X.shape[0] * X.shape[1] * C
     achieved = flop / (pot_ms / 1e3) / 1e12
-    # DRAM bytes (read + write) of one launch of the dominant kernel at exactly this workload, from the
-    # ncu capture summarised in profiles/ (logreg_tc_kernel / logreg_simt_kernel, 1024 chains)
-    traffic = None
-    if X.shape == (581012, 55) and C == 1024:
-        traffic = 77.08e6 if precision == "bf16x3" else 135.3e6
+    # DRAM bytes (read + write) of one launch of the dominant kernel, from the ncu capture summarised
+    # in profiles/ for this kernel at 1024 chains
+    traffic, traffic_src = profiled_traffic(
+        "logreg_tc_kernel_covtype_1024chains" if precision == "bf16x3" else "logreg_simt_kernel_covtype_1024chains",
+        X.shape[0])
+    if C != 1024:
+        traffic, traffic_src = None, None
     roofline = {"bound": "tensor", "achieved": achieved, "peak": burst, "unit": "TFLOP/s",
-                "frac": achieved / burst, "traffic": traffic, "traffic_unit": "bytes per launch (ncu capture)",
+                "frac": achieved / burst, "traffic": traffic, "traffic_unit": "bytes per launch",
+                "traffic_source": traffic_src,
                 "peak_kind": peak_kind + " burst bf16",
                 "kernel": "logreg potential (%s)" % precision, "algorithmic_flop_per_launch": flop,
                 "launch_ms": pot_ms}
@@ -419,6 +522,29 @@ def main():
     if not args.no_e2e:
         log("e2e")
         e2e = _e2e(kernel, state, args.steps, B)
+    # ---------------- the configuration's full run: 500 warmup + 1000 sampling iterations
+    full, zfull = None, None
+    if args.full_samples > 0:
+        log("full run: %d sampling iterations" % args.full_samples)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        out = kernel.run_device(state, args.full_samples, collect=("z", "num_steps"))
+        b.record()
+        b.synchronize()
+        samp_ms = a.elapsed_time(b)
+        full_evals = int(out["num_steps"].sum().item())
+        zfull = out["z"].cpu().numpy()
+        del out
+        ess_f, rhat_f = min_bulk_ess(zfull)
+        if dist:
+            samp_ms, ess_f, full_evals = reduce_over_ranks(dist, samp_ms, ess_f, full_evals, device="cuda")
+        full = {"num_warmup": args.num_warmup, "num_samples": args.full_samples, "warmup_s": warmup_ms / 1e3,
+                "sampling_s": samp_ms / 1e3, "min_bulk_ess": ess_f,
+                "min_bulk_ess_per_s_total": ess_f / ((warmup_ms + samp_ms) / 1e3),
+                "min_bulk_ess_per_s_sampling": ess_f / (samp_ms / 1e3), "rhat_max": rhat_f,
+                "grad_evals_per_s_sampling": full_evals / (samp_ms / 1e3),
+                "definition": "min over the 55 coefficients of bulk-ESS of all post-warmup draws, divided by "
+                              "warmup + sampling seconds (total) or sampling seconds"}
     plain = None
     if args.plain_steps > 0 and world == 1:
         log("plain engine comparison")
@@ -436,7 +562,7 @@ def main():
         "min_bulk_ess": ess, "rhat_max": rhat, "warmup_s": warmup_ms / 1e3,
         "setup_s": time.perf_counter() - t0,
         "roofline": roofline, "clocks": clk, "gpu_launches": int(ticks * _launches_per_tick(precision)),
-        "e2e": e2e, "plain_engine": plain,
+        "e2e": e2e, "plain_engine": plain, "full_run": full,
     }
     if rank == 0 and not args.no_cpu and world == 1:
         try:
@@ -447,11 +573,29 @@ def main():
             line["cpu_baseline"] = cpu_baseline(X, y, chains=nc, num_samples=args.cpu_samples, init=init)
         except Exception as ex:  # the baseline is reported, never required for the GPU number
             line["cpu_baseline"] = {"value": None, "error": str(ex)[:200]}
+        if args.oracle_samples > 0 and zfull is not None:
+            try:
+                log("FP64 oracle posterior check")
+                line["posterior_vs_fp64_oracle"] = oracle_moment_check(X, y, state, zfull, nc, args.oracle_samples)
+            except Exception as ex:
+                line["posterior_vs_fp64_oracle"] = {"error": str(ex)[:200]}
+    del zfull
+    if rank == 0 and not args.no_workloads and world == 1:
+        kernel.close()
+        kernel = None
+        line["workloads"] = {}
+        for w, prec in (("eight_schools", None), ("uneven_hier", None),
+                        ("horseshoe_nc", "bf16x3" if _tc_available() else None), ("sv", None)):
+            try:
+                line["workloads"][w] = workload_run(w, prec)
+            except Exception as ex:
+                line["workloads"][w] = {"error": str(ex)[:200]}
     if rank == 0:
         print(json.dumps(line))
     if dist:
         dist.destroy_process_group()
-    kernel.close()
+    if kernel is not None:
+        kernel.close()
     return 0
 
 
@@ -470,7 +614,10 @@ def _launches_per_tick(precision):
     return 4 if precision == "bf16x3" else 3
 
 
-def _time_potential(kernel, state, reps=10):
+def _time_potential(kernel, state, reps=10, batch=20):
+    """Average duration of one potential launch (for the tensor-core path: coefficient split,
+    tcgen05 kernel and row-group finish), from CUDA events on the kernel's stream around
+    ``batch`` back-to-back launches, as the tick loop issues them; median over ``reps`` batches."""
     import torch
 
     z = state.z.clone()
@@ -480,11 +627,31 @@ def _time_potential(kernel, state, reps=10):
     for _ in range(reps):
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         a.record()
-        kernel.potential_and_grad(z)
+        for _ in range(batch):
+            kernel.potential_and_grad(z)
         b.record()
         b.synchronize()
-        ts.append(a.elapsed_time(b))
+        ts.append(a.elapsed_time(b) / batch)
     return float(np.median(ts))
+
+
+def profiled_traffic(kernel_name, n_rows):
+    """DRAM bytes (read + write) of one launch of a profiled kernel, from the ncu summary in
+    profiles/ (its ``traffic_bytes_per_launch`` line, captured at ``rows``); scaled to n_rows
+    rows, since the launch streams the design matrix once."""
+    import re
+
+    path = os.path.join(ROOT, "profiles", kernel_name + ".md")
+    try:
+        text = open(path).read()
+    except OSError:
+        return None, None
+    m = re.search(r"traffic_bytes_per_launch\s*=\s*([0-9.eE+]+)\s*\(rows\s*=\s*([0-9]+)", text)
+    if not m:
+        return None, None
+    t, rows = float(m.group(1)), int(m.group(2))
+    return t * n_rows / rows, "ncu capture (%s), %d rows%s" % (
+        os.path.basename(path), rows, "" if rows == n_rows else ", scaled to %d rows" % n_rows)
 
 
 def _state_leaves(st):

@@ -96,6 +96,7 @@ typedef struct {
   const float* sigma;
   const int32_t* offsets;
   double hyper[4];
+  int32_t row_threads; /* logistic family: threads sharing one chain's rows (0/1: none) */
 } nutsref_model;
 
 int nutsref_latent_dim(const nutsref_model* m, int model_index) {
@@ -131,48 +132,136 @@ static double digamma_ref(double x) {
   return acc + log(x) - 0.5 / x + t;
 }
 
-/* numpyro potential_energy of the logistic model (examples/covtype.py:66-71):
- * one fused pass over the rows; per-row arithmetic in `real`, sums in double. */
-#define LR_BLOCK 256
-static double logreg_pg(const nutsref_model* m, const real* b, real* g) {
-  int D = m->P;
-  double ll = 0.0;
-  double* ga = (double*)calloc((size_t)D, sizeof(double));
-  real* gb = (real*)calloc((size_t)D, sizeof(real));
-  for (int64_t n0 = 0; n0 < m->N; n0 += LR_BLOCK) {
-    int64_t n1 = n0 + LR_BLOCK < m->N ? n0 + LR_BLOCK : m->N;
-    real llb = 0;
-    for (int64_t n = n0; n < n1; ++n) {
-      const float* x = m->X + n * D;
-      real l = 0;
-      for (int d = 0; d < D; ++d) l += (real)x[d] * b[d];
 #if REAL_IS_FLOAT
-      real t = expf(-fabsf(l));
-      real sp = (l > 0 ? l : 0.0f) + log1pf(t);
-#else
-      real t = exp(-fabs(l));
-      real sp = (l > 0 ? l : 0.0) + log1p(t);
+/* FP32 transcendentals written so a compiler can vectorise the row loop (libm calls would stay
+ * scalar), as XLA's CPU backend does for numpyro's float32 potential:
+ *   exp: Cody & Waite (1980) range reduction x = k ln2 + r, |r| <= ln2/2, with the degree-6 Taylor
+ *        polynomial of e^r (truncation error 0.347^7 / 7! = 1.2e-7 relative);
+ *   log1p: log(1 + t) = 2 atanh(s), s = t / (2 + t) in [0, 1/3] for t in [0, 1], by the odd series
+ *        2 (s + s^3/3 + ... + s^13/13) (Abramowitz & Stegun 4.1.28; truncation error < 2e-8). */
+static inline float exp_neg_f(float x) { /* e^x for x <= 0 */
+  x = x < -87.0f ? -87.0f : x;
+  const float kf = (x * 1.44269504088896341f + 12582912.0f) - 12582912.0f;
+  const float r = (x - kf * 0.693145751953125f) - kf * 1.428606765330187e-06f;
+  float p = 1.0f / 720.0f;
+  p = p * r + 1.0f / 120.0f;
+  p = p * r + 1.0f / 24.0f;
+  p = p * r + 1.0f / 6.0f;
+  p = p * r + 0.5f;
+  p = p * r + 1.0f;
+  p = p * r + 1.0f;
+  union { float f; int32_t i; } u;
+  u.i = ((int32_t)kf + 127) << 23;
+  return p * u.f;
+}
+static inline float log1p_unit_f(float t) { /* log(1 + t) for t in [0, 1] */
+  const float s = t / (2.0f + t), s2 = s * s;
+  float q = 1.0f / 13.0f;
+  q = q * s2 + 1.0f / 11.0f;
+  q = q * s2 + 1.0f / 9.0f;
+  q = q * s2 + 1.0f / 7.0f;
+  q = q * s2 + 1.0f / 5.0f;
+  q = q * s2 + 1.0f / 3.0f;
+  q = q * s2 + 1.0f;
+  return 2.0f * s * q;
+}
 #endif
-      real sig = l >= 0 ? (real)1 / ((real)1 + t) : t / ((real)1 + t);
-      real yy = (real)m->y[n];
+
+/* numpyro potential_energy of the logistic model (examples/covtype.py:66-71): rows [n0, n1) into
+ * double partials ga (gradient of the log-likelihood part) and *ll; per-row arithmetic in `real`,
+ * blocks of LR_BLOCK rows flushed into the double accumulators. */
+#define LR_BLOCK 256
+static void logreg_rows(const nutsref_model* m, const real* b, int64_t r0, int64_t r1, double* ga, double* ll) {
+  const int D = m->P;
+  real gb[64];
+  real lb[LR_BLOCK], eb[LR_BLOCK];
+  double lls = 0.0;
+  for (int d = 0; d < D; ++d) gb[d] = 0;
+  for (int64_t n0 = r0; n0 < r1; n0 += LR_BLOCK) {
+    const int nb = (int)(n0 + LR_BLOCK < r1 ? LR_BLOCK : r1 - n0);
+    const float* xb = m->X + n0 * D;
+    for (int r = 0; r < nb; ++r) {
+      const float* x = xb + (int64_t)r * D;
+      real l = 0;
+#pragma omp simd reduction(+ : l)
+      for (int d = 0; d < D; ++d) l += (real)x[d] * b[d];
+      lb[r] = l;
+    }
+    real llb = 0;
+#if REAL_IS_FLOAT
+#pragma omp simd reduction(+ : llb)
+    for (int r = 0; r < nb; ++r) {
+      const real l = lb[r], yy = (real)m->y[n0 + r];
+      const real t = exp_neg_f(-fabsf(l));
+      const real sp = (l > 0 ? l : 0.0f) + log1p_unit_f(t);
+      const real inv = 1.0f / (1.0f + t);
+      const real sig = l >= 0 ? inv : t * inv;
       llb += sp - yy * l;
-      real e = sig - yy;
+      eb[r] = sig - yy;
+    }
+#else
+    for (int r = 0; r < nb; ++r) {
+      const real l = lb[r], yy = (real)m->y[n0 + r];
+      const real t = exp(-fabs(l));
+      const real sp = (l > 0 ? l : 0.0) + log1p(t);
+      const real sig = l >= 0 ? (real)1 / ((real)1 + t) : t / ((real)1 + t);
+      llb += sp - yy * l;
+      eb[r] = sig - yy;
+    }
+#endif
+    for (int r = 0; r < nb; ++r) {
+      const float* x = xb + (int64_t)r * D;
+      const real e = eb[r];
+#pragma omp simd
       for (int d = 0; d < D; ++d) gb[d] += e * (real)x[d];
     }
     /* block partial sums (<= 256 rows) are flushed into double accumulators */
-    ll += (double)llb;
+    lls += (double)llb;
     for (int d = 0; d < D; ++d) {
       ga[d] += (double)gb[d];
       gb[d] = 0;
     }
   }
-  free(gb);
+  *ll += lls;
+}
+
+/* With row_threads > 1 the rows are split into that many contiguous ranges evaluated by an OpenMP
+ * team (the chains then run one after another), and the ranges' partials are added in order. */
+static double logreg_pg(const nutsref_model* m, const real* b, real* g) {
+  const int D = m->P;
+  double ll = 0.0;
+  double ga[64];
+  for (int d = 0; d < D; ++d) ga[d] = 0.0;
+  const int T = m->row_threads > 1 ? m->row_threads : 1;
+  if (T == 1) {
+    logreg_rows(m, b, 0, m->N, ga, &ll);
+  } else {
+    double part[T][65];
+#pragma omp parallel num_threads(T)
+    {
+#ifdef _OPENMP
+      const int k = omp_get_thread_num(), nt = omp_get_num_threads();
+#else
+      const int k = 0, nt = 1;
+#endif
+      const int64_t per = (m->N + T - 1) / T;
+      for (int kk = k; kk < T; kk += nt) {
+        double* pp = part[kk];
+        for (int d = 0; d <= D; ++d) pp[d] = 0.0;
+        const int64_t a = (int64_t)kk * per, e = a + per < m->N ? a + per : m->N;
+        if (a < e) logreg_rows(m, b, a, e, pp, &pp[D]);
+      }
+    }
+    for (int kk = 0; kk < T; ++kk) {
+      for (int d = 0; d < D; ++d) ga[d] += part[kk][d];
+      ll += part[kk][D];
+    }
+  }
   double pr = 0.0, s = m->hyper[0] > 0 ? m->hyper[0] : 1.0;
   for (int d = 0; d < D; ++d) {
     g[d] = (real)(ga[d] + (double)b[d] / (s * s));
     pr += 0.5 * (double)b[d] * (double)b[d] / (s * s) + 0.5 * log(2 * M_PI) + log(s);
   }
-  free(ga);
   return ll + pr;
 }
 
@@ -562,7 +651,7 @@ int nutsref_transitions(const nutsref_model* m, int chains, const uint32_t* chai
 #ifdef _OPENMP
   if (threads > 0) omp_set_num_threads(threads);
 #endif
-#pragma omp parallel for schedule(dynamic, 1)
+#pragma omp parallel for schedule(dynamic, 1) if (m->row_threads <= 1)
   for (int k = 0; k < chains; ++k) {
     chain_t c;
     memset(&c, 0, sizeof(c));
@@ -637,7 +726,7 @@ int nutsref_run_model(const nutsref_model* m, int ld, int chains, int first_chai
     c->ss[4] = log(10.0 * c->step);
   }
   tw0 = now_s();
-#pragma omp parallel for schedule(dynamic, 1) reduction(+ : gw)
+#pragma omp parallel for schedule(dynamic, 1) reduction(+ : gw) if (m->row_threads <= 1)
   for (int k = 0; k < chains; ++k) {
     chain_t* c = &cs[k];
     c->pe = potential_grad(m, c->k, c->z, c->g);
@@ -654,7 +743,7 @@ int nutsref_run_model(const nutsref_model* m, int ld, int chains, int first_chai
     c->grad_evals = 0;
   }
   tw1 = now_s();
-#pragma omp parallel for schedule(dynamic, 1) reduction(+ : gs)
+#pragma omp parallel for schedule(dynamic, 1) reduction(+ : gs) if (m->row_threads <= 1)
   for (int k = 0; k < chains; ++k) {
     chain_t* c = &cs[k];
     uint32_t chain = (uint32_t)(first_chain + k);

@@ -65,16 +65,20 @@ def typical_points(name, model, rng, C):
     return rng.uniform(-2, 2, (C, D)).astype(np.float32)
 
 
-def replay_parity(kernel, state, cmodel, seed, transitions, max_tree_depth=10, threads=0):
+def replay_parity(kernel, state, cmodel, seed, transitions, max_tree_depth=10, threads=0, fp32_oracle=False):
     """Runs ``transitions`` GPU transitions of ``kernel`` from ``state`` (after warmup, so
     without adaptation) and replays each one with the FP64 C oracle from the GPU's own
     starting state (position, step size, mass rows) at the same Philox stream addresses.
     Returns counts of identical tree sizes / divergence flags and the relative position
-    errors of the transitions whose tree sizes agree."""
+    errors of the transitions whose tree sizes agree.  With ``fp32_oracle`` the FP32 build of
+    the same C restatement (numpyro's algorithm in its float32 dtype) is replayed from the
+    same states too, and its agreement with FP64 is counted as ``same32``: how far float32
+    rounding alone moves the tree decisions of this model."""
     from oracle import build_oracle as B
 
     lib = B.load("f64")
-    same, total, zerr, aperr, st = 0, 0, [], [], state
+    lib32 = B.load("f32") if fp32_oracle else None
+    same, same32, total, zerr, aperr, zerr32, aperr32, st = 0, 0, 0, [], [], [], [], state
     for _ in range(transitions):
         z0 = st.z.cpu().numpy()
         step = st.adapt_state.step_size.cpu().numpy()
@@ -88,6 +92,15 @@ def replay_parity(kernel, state, cmodel, seed, transitions, max_tree_depth=10, t
         ap = new.accept_prob.cpu().numpy()
         ref = B.transitions(lib, cmodel, z0, step, inv, msq, key[:, 0], key[:, 1], seed,
                             max_tree_depth=max_tree_depth, threads=threads)
+        if lib32 is not None:
+            r32 = B.transitions(lib32, cmodel, z0, step, inv, msq, key[:, 0], key[:, 1], seed,
+                                max_tree_depth=max_tree_depth, threads=threads)
+            agree32 = (r32["num_steps"] == ref["num_steps"]) & (r32["diverging"] == ref["diverging"])
+            same32 += int(np.sum(agree32))
+            for c in np.nonzero(agree32)[0]:
+                rz = ref["z"][c].astype(np.float64)
+                zerr32.append(np.max(np.abs(rz - r32["z"][c]) / (np.abs(rz) + 1e-2)))
+                aperr32.append(abs(ref["accept_prob"][c] - r32["accept_prob"][c]))
         for c in range(z0.shape[0]):
             total += 1
             if ref["num_steps"][c] == ns[c] and ref["diverging"][c] == dv[c]:
@@ -97,7 +110,8 @@ def replay_parity(kernel, state, cmodel, seed, transitions, max_tree_depth=10, t
                 zerr.append(np.max(np.abs(rz - zg[c]) / (np.abs(rz) + 1e-2)))
         st = new
     return {"same": same, "total": total, "frac": same / total, "zerr": np.array(zerr), "aperr": np.array(aperr),
-            "state": st}
+            "state": st, "same32": same32 if lib32 is not None else None, "zerr32": np.array(zerr32),
+            "aperr32": np.array(aperr32)}
 
 
 def cmodel_of(model, chains_per_model=1):

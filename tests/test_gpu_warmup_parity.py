@@ -92,7 +92,8 @@ def _run_across(k, st, pot, until, steps, C, **kw):
             np.testing.assert_allclose(g["msq"][c], a.mass_matrix_sqrt, rtol=1e-4,
                                        err_msg="chain %d step %d" % (c, s))
             assert g["n"][c] == a.mm_state[2], (c, s)
-            np.testing.assert_allclose(g["ss"][c][4], a.ss_state[4], rtol=1e-5, atol=1e-6)
+            # the prox centre log(10 step) carries the step size's relative error as an absolute one
+            np.testing.assert_allclose(g["ss"][c][4], a.ss_state[4], rtol=0, atol=2e-4)
         agree += ok
     return agree, cur
 
