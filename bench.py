@@ -361,15 +361,36 @@ def oracle_moment_check(X, y, state, zgpu, chains, transitions):
             "oracle_min_bulk_ess": float(eo.min())}
 
 
+def reference_leg(X, y, chains, num_warmup, num_samples, cores, budget_s=300.0):
+    """The reference arm's timed CPU work: numpyro's NUTS as the FP32 C restatement (numpyro's
+    default dtype) on the host cores, from init_to_uniform with the Stan warmup, ``chains``
+    chains one after another, each evaluating its potential on all ``cores`` threads (rows
+    split across the threads, as XLA's CPU backend splits one chain's matrix products)."""
+    from oracle import build_oracle
+
+    lib = build_oracle.load("f32")
+    model = build_oracle.Model("logreg", X=X, y=y, row_threads=cores)
+    res = build_oracle.run_model(lib, model, X.shape[1], chains, num_warmup, num_samples, seed=0, threads=cores,
+                                 warmup_budget_s=budget_s)
+    ess, rhat = min_bulk_ess(res["samples"])
+    sample = ("%d of the 1024 chains: init_to_uniform, %d-iteration Stan warmup (%.0f s, %s), then %d sampling "
+              "transitions each (max_tree_depth 10) on the full N=%d x %d data; FP32 C restatement of numpyro's "
+              "NUTS with each chain's potential split across %d host threads; ESS/s = min bulk-ESS of the sampling "
+              "draws / sampling seconds" % (chains, num_warmup, res["warmup_s"],
+                                            "completed" if res["warmup_s"] < budget_s else "cut at the time budget",
+                                            num_samples, X.shape[0], X.shape[1], cores))
+    return {"value": ess / res["sampling_s"], "unit": "ESS/s", "cores": cores, "kind": "port", "sample": sample,
+            "grad_evals_per_s": res["sampling_grad_evals"] / res["sampling_s"], "sampling_s": res["sampling_s"],
+            "warmup_s": res["warmup_s"], "warmup_grad_evals": res["warmup_grad_evals"], "min_bulk_ess": ess,
+            "rhat_max": rhat}
+
+
 def run_reference(args):
     """--impl reference: numpyro itself cannot run here (no jax); its NUTS algorithm runs as the
-    C restatement (FP32 build, numpyro's default dtype) on the host cores, on the workload of our
-    arm: the same 500-iteration Stan warmup from init_to_uniform, then --steps sampling steps of
-    --iters-per-step transitions.  A bounded sample of the 1024 chains: 4 chains, each evaluating
-    its potential on all host threads (rows split across the threads, as XLA's CPU backend splits
-    one chain's matrix products), run one after another."""
+    C restatement on the host cores, on the workload of our arm: the same 500-iteration Stan
+    warmup, then --steps sampling steps of --iters-per-step transitions, on a bounded sample of
+    4 of the 1024 chains (reference_leg)."""
     from numpyro_gb300 import datasets
-    from oracle import build_oracle
 
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -377,30 +398,15 @@ def run_reference(args):
     X, y, _ = datasets.covtype_like(seed=0, n=args.n)
     cores = len(os.sched_getaffinity(0))
     chains = 4
-    B = args.iters_per_step
+    B = getattr(args, "iters_per_step", 10)
     S = max(4, args.steps * B)
-    lib = build_oracle.load("f32")
-    model = build_oracle.Model("logreg", X=X, y=y, row_threads=cores)
-    budget_s = 300.0
-    res = build_oracle.run_model(lib, model, X.shape[1], chains, args.num_warmup, S, seed=0, threads=cores,
-                                 warmup_budget_s=budget_s)
-    ess, rhat = min_bulk_ess(res["samples"])
-    value = ess / res["sampling_s"]
-    sample = ("%d of the 1024 chains: init_to_uniform, %d-iteration Stan warmup (%.0f s, %s), then %d sampling "
-              "transitions each (max_tree_depth 10) on the full N=%d x %d data; FP32 C restatement of numpyro's "
-              "NUTS with each chain's potential split across %d host threads; ESS/s = min bulk-ESS of the sampling "
-              "draws / sampling seconds" % (chains, args.num_warmup, res["warmup_s"],
-                                            "completed" if res["warmup_s"] < budget_s else "cut at the time budget",
-                                            S, X.shape[0], X.shape[1], cores))
-    cb = {"value": value, "unit": "ESS/s", "cores": cores, "kind": "port", "sample": sample,
-          "grad_evals_per_s": res["sampling_grad_evals"] / res["sampling_s"], "sampling_s": res["sampling_s"],
-          "warmup_s": res["warmup_s"], "warmup_grad_evals": res["warmup_grad_evals"], "min_bulk_ess": ess,
-          "rhat_max": rhat}
+    num_warmup = getattr(args, "num_warmup", 500)
+    cb = reference_leg(X, y, chains, num_warmup, S, cores)
+    value = cb["value"]
     line = {"metric": METRIC, "value": value, "unit": "ESS/s", "impl": "reference", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * res["sampling_s"] / max(1, args.steps),
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * cb["sampling_s"] / max(1, args.steps),
             "higher_is_better": True, "scaling": "weak", "dtype": "f32", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "chains_timed": chains, "iters_per_step": B,
-                       "num_warmup": args.num_warmup},
+            "config": {"workload": WORKLOAD, "chains_timed": chains, "iters_per_step": B, "num_warmup": num_warmup},
             "cpu_baseline": cb,
             "e2e": {"value": value, "unit": "ESS/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "grad_evals_per_s": cb["grad_evals_per_s"], "vs_baseline": None}

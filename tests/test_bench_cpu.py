@@ -19,7 +19,7 @@ def test_reference_arm_line_keys(monkeypatch, capsys):
     b = _bench()
     fake = {"value": 20.0, "unit": "ESS/s", "cores": 16, "kind": "port", "grad_evals_per_s": 500.0,
             "sampling_s": 40.0, "sample": "stub"}
-    monkeypatch.setattr(b, "cpu_baseline", lambda *a, **k: dict(fake))
+    monkeypatch.setattr(b, "reference_leg", lambda *a, **k: dict(fake))
     monkeypatch.setenv("RANK", "0")
     args = types.SimpleNamespace(n=1000, steps=3, warmup=1, gpus=1)
     assert b.run_reference(args) == 0
@@ -35,7 +35,7 @@ def test_reference_arm_line_keys(monkeypatch, capsys):
 def test_reference_arm_other_ranks_print_nothing(monkeypatch, capsys):
     b = _bench()
     monkeypatch.setenv("RANK", "1")
-    monkeypatch.setattr(b, "cpu_baseline", lambda *a, **k: (_ for _ in ()).throw(AssertionError("ran")))
+    monkeypatch.setattr(b, "reference_leg", lambda *a, **k: (_ for _ in ()).throw(AssertionError("ran")))
     assert b.run_reference(types.SimpleNamespace(n=1000, steps=3, warmup=1, gpus=2)) == 0
     assert capsys.readouterr().out == ""
 
