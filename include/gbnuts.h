@@ -159,6 +159,12 @@ const char* gbn_last_error(gbn_handle h); /* h may be NULL: last global error */
 
 int gbn_create(gbn_handle* out, const gbn_model_desc* model, const gbn_config* cfg);
 int gbn_destroy(gbn_handle h);
+/* Integer id of a handle (unique in the process, assigned by gbn_create; 0 for NULL) and the
+ * handle of an id (NULL once destroyed), thread-safe: for callers that pass a handle as a plain
+ * attribute, such as an XLA FFI handler bound through jax.ffi (numpyro's sample runs under jit,
+ * numpyro/infer/mcmc.py:188-190), which XLA may invoke from any thread. */
+int64_t gbn_handle_id(gbn_handle h);
+gbn_handle gbn_handle_from_id(int64_t id);
 int gbn_latent_dim(gbn_handle h, int32_t* dim);
 
 /* U(z) and dU/dz for num_points latent vectors (device pointers). */
@@ -176,6 +182,19 @@ int gbn_init(gbn_handle h, void* stream, int32_t num_warmup, const float* d_init
 
 /* One transition for every chain (MCMCKernel.sample). */
 int gbn_sample(gbn_handle h, void* stream, gbn_state* st);
+
+/* The same transition, enqueued on `stream` with no host synchronisation, for callers that
+ * trace sample(): numpyro runs it under jit (numpyro/infer/mcmc.py:188-190, util.py:386-403),
+ * where an XLA FFI handler must not block the host.  The tick engine's loop runs on the device:
+ * a CUDA graph whose WHILE node repeats batches of ticks until no chain is active, bounded by a
+ * tick budget; the hierarchical and stochastic-volatility families are one persistent launch.
+ * The first call on a handle builds that graph (a synchronous set-up). Draws and states are
+ * bit-identical to gbn_sample.  A budget exhausted or a device wait timed out is recorded on the
+ * device and reported by gbn_check_async. */
+int gbn_sample_async(gbn_handle h, void* stream, gbn_state* st);
+/* Synchronises `stream` and returns GBN_ERR_TIMEOUT if an earlier gbn_sample_async ran out of
+ * its tick budget or a tensor-core wait timed out (the error is then cleared), else GBN_OK. */
+int gbn_check_async(gbn_handle h, void* stream);
 
 /* num_iterations transitions per chain; iteration j (0-based, this call) is
  * collected when j >= collect_start and (j - collect_start) % thinning == 0. */

@@ -130,6 +130,8 @@ EXPORTS = {
     "gbn_init": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p,
                                 ctypes.POINTER(State)]),
     "gbn_sample": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(State)]),
+    "gbn_sample_async": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(State)]),
+    "gbn_check_async": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
     "gbn_run": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(State), ctypes.c_int32,
                                ctypes.c_int32, ctypes.c_int32, ctypes.POINTER(Collect)]),
     "gbn_get_stats": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Stats)]),
@@ -139,6 +141,8 @@ EXPORTS = {
                                                     ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p,
                                                     ctypes.c_void_p]),
     "gbn_noalloc_last_error": (ctypes.c_char_p, []),
+    "gbn_handle_id": (ctypes.c_int64, [ctypes.c_void_p]),
+    "gbn_handle_from_id": (ctypes.c_void_p, [ctypes.c_int64]),
 }
 NOALLOC_MAX_POINTS = 256  # GBN_NOALLOC_MAX_POINTS in include/gbnuts.h
 

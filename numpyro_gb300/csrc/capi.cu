@@ -11,6 +11,8 @@
 #include <algorithm>
 #include <cstdlib>
 #include <cstring>
+#include <map>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -50,11 +52,21 @@ struct gbn_handle_s {
   cudaGraphExec_t tick_graph = nullptr;
   void* graph_scratch = nullptr;  // potential scratch the graph was captured with
   std::string tuning;             // launch shapes chosen by the autotuner
+  int64_t id = 0;                 // registry id (gbn_handle_id)
   double* vjp_pe = nullptr;       // potential values discarded by gbn_potential_vjp
   int vjp_cap = 0;
+  // gbn_sample_async: a graph whose WHILE node repeats tick batches until no chain is active
+  cudaGraphExec_t async_graph = nullptr;
+  int32_t* async_iter = nullptr;  // [2]: loop iterations done, iteration budget
 };
 
 static thread_local std::string g_last_error;
+
+// Integer ids of live handles, for callers that can pass a handle only as a plain attribute (an
+// XLA FFI handler bound through jax.ffi, which XLA may call from any thread).
+static std::mutex g_handles_mu;
+static std::map<int64_t, gbn_handle> g_handles;
+static int64_t g_next_id = 1;
 
 static int fail(gbn_handle h, int code, const std::string& msg) {
   g_last_error = msg;
@@ -157,8 +169,20 @@ int gbn_latent_dim(gbn_handle h, int32_t* dim) {
   return GBN_OK;
 }
 
+int64_t gbn_handle_id(gbn_handle h) { return h ? h->id : 0; }
+
+gbn_handle gbn_handle_from_id(int64_t id) {
+  std::lock_guard<std::mutex> lock(g_handles_mu);
+  auto it = g_handles.find(id);
+  return it == g_handles.end() ? nullptr : it->second;
+}
+
 int gbn_destroy(gbn_handle h) {
   if (!h) return GBN_OK;
+  if (h->id) {
+    std::lock_guard<std::mutex> lock(g_handles_mu);
+    g_handles.erase(h->id);
+  }
   cudaDeviceSynchronize();
   if (h->m.tc) logreg_tc_free(h->m);
   if (h->m.hs_tc) horseshoe_tc_free(h->m);
@@ -168,6 +192,7 @@ int gbn_destroy(gbn_handle h) {
   if (h->ev0) cudaEventDestroy(h->ev0);
   if (h->ev1) cudaEventDestroy(h->ev1);
   if (h->tick_graph) cudaGraphExecDestroy(h->tick_graph);
+  if (h->async_graph) cudaGraphExecDestroy(h->async_graph);
   if (h->cap_stream) cudaStreamDestroy(h->cap_stream);
   delete h;
   return GBN_OK;
@@ -352,6 +377,9 @@ int gbn_create(gbn_handle* out, const gbn_model_desc* md, const gbn_config* cfg)
   if (ce == cudaSuccess) ce = dalloc(h, &h->dP, 1);
   if (ce == cudaSuccess) ce = dalloc(h, &h->vjp_pe, (size_t)C);
   h->vjp_cap = C;
+  if (ce == cudaSuccess) ce = dalloc(h, &h->async_iter, 2);
+  if (ce == cudaSuccess) ce = dalloc(h, &h->done_count, 2);  // one transition: gbn_sample(_async)
+  h->done_cap = 2;
   if (ce == cudaSuccess) ce = cudaMallocHost((void**)&h->h_counters, sizeof(int32_t) * 8);
   if (ce == cudaSuccess) ce = cudaEventCreate(&h->ev0);
   if (ce == cudaSuccess) ce = cudaEventCreate(&h->ev1);
@@ -380,6 +408,8 @@ int gbn_create(gbn_handle* out, const gbn_model_desc* md, const gbn_config* cfg)
     ce = horseshoe_tc_prepare(m, C);
   }
   if (ce == cudaSuccess) ce = ensure_potential_scratch(m, C);
+  if (ce == cudaSuccess && m.family == GBN_FAMILY_LOGREG && !(m.precision == GBN_PREC_BF16X3 && m.tc))
+    ce = logreg_simt_smem_attr();  // before any graph capture of its launches
   if (ce != cudaSuccess) {
     int r = cuda_fail(nullptr, ce, "gbn_create: allocation");
     gbn_destroy(h);
@@ -422,6 +452,11 @@ int gbn_create(gbn_handle* out, const gbn_model_desc* md, const gbn_config* cfg)
   P.counters = h->counters;
   P.error_word = h->err_word;
   P.thinning = 1;
+  {
+    std::lock_guard<std::mutex> lock(g_handles_mu);
+    h->id = g_next_id++;
+    g_handles[h->id] = h;
+  }
   *out = h;
   return GBN_OK;
 }
@@ -681,6 +716,104 @@ int gbn_run(gbn_handle h, void* stream, gbn_state* st, int32_t num_iterations, i
 }
 
 int gbn_sample(gbn_handle h, void* stream, gbn_state* st) { return gbn_run(h, stream, st, 1, 0, 1, nullptr); }
+
+// Builds the graph of gbn_sample_async's tick loop: a WHILE node whose body is one batch of
+// ticks followed by the condition kernel.  Every kernel reads its parameters from device memory
+// (the AdvParams block, the counters), so one graph serves every later call of the handle.
+static cudaError_t build_async_graph(gbn_handle h) {
+  cudaGraph_t g = nullptr;
+  cudaError_t e = cudaGraphCreate(&g, 0);
+  cudaGraphConditionalHandle ch = 0;
+  if (e == cudaSuccess) e = cudaGraphConditionalHandleCreate(&ch, g, 1, cudaGraphCondAssignDefault);
+  cudaGraphNodeParams np = {};
+  np.type = cudaGraphNodeTypeConditional;
+  np.conditional.handle = ch;
+  np.conditional.type = cudaGraphCondTypeWhile;
+  np.conditional.size = 1;
+  cudaGraphNode_t node = nullptr;
+  if (e == cudaSuccess) e = cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &np);
+  if (e == cudaSuccess) {
+    cudaGraph_t body = np.conditional.phGraph_out[0];
+    e = cudaStreamBeginCaptureToGraph(h->cap_stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) {
+      cudaError_t el = launch_tick_batch(h, h->cap_stream);
+      const int* tc_err = h->m.tc ? logreg_tc_error_ptr(h->m) : (h->m.hs_tc ? horseshoe_tc_error_ptr(h->m) : nullptr);
+      launch_tick_condition((unsigned long long)ch, h->counters, (TICK_BATCH - 1) & 1, h->async_iter, tc_err,
+                            h->err_word, h->cap_stream);
+      e = cudaStreamEndCapture(h->cap_stream, &body);
+      if (el != cudaSuccess) e = el;
+    }
+  }
+  if (e == cudaSuccess) e = cudaGraphInstantiate(&h->async_graph, g, 0);
+  if (g) cudaGraphDestroy(g);
+  if (e != cudaSuccess) {
+    h->async_graph = nullptr;
+    cudaGetLastError();
+  }
+  return e;
+}
+
+int gbn_sample_async(gbn_handle h, void* stream, gbn_state* st) {
+  if (!h || !state_ok(st)) return fail(h, GBN_ERR_INVALID_ARG, "gbn_sample_async: bad argument");
+  if (!h->window_end) return fail(h, GBN_ERR_INVALID_ARG, "gbn_sample_async: call gbn_init first");
+  cudaStream_t s = (cudaStream_t)stream;
+  AdvParams& P = h->hp;
+  fill_state(P, st);
+  P.col = CollectBufs{};
+  P.collect_start = 0;
+  P.thinning = 1;
+  P.num_collect = 0;
+  P.done_count = h->done_count;  // sized for one transition at gbn_create
+  cudaError_t e = cudaSuccess;
+  if (!h->persistent && !h->async_graph) {  // first call of the handle: build the tick-loop graph
+    int64_t per_iter = (h->cfg.algo == GBN_ALGO_HMC) ? 4096 : ((int64_t)1 << h->maxd) + 8;
+    if (h->cfg.find_heuristic_step_size) per_iter += 512;
+    const int64_t max_ticks = per_iter * (P.lockstep ? 2 : 1) + 4096;
+    const int32_t budget[2] = {0, (int32_t)(max_ticks / TICK_BATCH + 1)};
+    e = cudaMemcpy(h->async_iter, budget, sizeof(budget), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = build_async_graph(h);
+    if (e != cudaSuccess) return cuda_fail(h, e, "gbn_sample_async: graph set-up");
+  }
+  launch_set_params(P, h->dP, s);
+  e = cudaMemsetAsync(h->done_count, 0, sizeof(int32_t) * 2, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(h->counters, 0, sizeof(int32_t) * 8, s);
+  if (e != cudaSuccess) return cuda_fail(h, e, "gbn_sample_async: setup");
+  launch_set_phase(h->dP, h->C, PH_START, 1, s);
+  if (h->persistent) {
+    if (h->m.family == GBN_FAMILY_SV) {
+      SvView sv{h->m.y, (int)h->m.n, h->m.hyper[2] != 0.0, h->m.hyper[0], h->m.hyper[1]};
+      launch_persistent_sv(h->dP, sv, h->counters + 7, h->C, h->D, s);
+    } else {
+      HierView hv{h->m.y, h->m.hier_sinv, h->m.hier_cmodel, h->m.offsets, h->m.chains_per_model, h->m.num_models,
+                  (float)(1.0 / (h->m.hyper[0] * h->m.hyper[0])), (float)(1.0 / h->m.hyper[1])};
+      launch_persistent_hier(h->dP, hv, h->counters + 7, h->order, h->C, h->hp.dense != 0, s);
+    }
+  } else {
+    e = cudaMemsetAsync(h->async_iter, 0, sizeof(int32_t), s);
+    if (e == cudaSuccess) e = cudaGraphLaunch(h->async_graph, s);
+    if (e != cudaSuccess) return cuda_fail(h, e, "gbn_sample_async: launch");
+  }
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(h, e, "gbn_sample_async");
+  return GBN_OK;
+}
+
+int gbn_check_async(gbn_handle h, void* stream) {
+  if (!h) return fail(h, GBN_ERR_INVALID_ARG, "gbn_check_async: null handle");
+  cudaStream_t s = (cudaStream_t)stream;
+  cudaError_t e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return cuda_fail(h, e, "gbn_check_async");
+  int32_t w = 0;
+  e = cudaMemcpy(&w, h->err_word, sizeof(int32_t), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_fail(h, e, "gbn_check_async");
+  if (w != 0) {
+    cudaMemset(h->err_word, 0, sizeof(int32_t));
+    return fail(h, GBN_ERR_TIMEOUT, "an asynchronous transition exhausted its tick budget or a device wait timed out");
+  }
+  if ((h->m.tc && logreg_tc_error(h->m)) || (h->m.hs_tc && horseshoe_tc_error(h->m)))
+    return fail(h, GBN_ERR_TIMEOUT, "tensor-core potential: a device wait timed out");
+  return GBN_OK;
+}
 
 const char* gbn_tuning(gbn_handle h) { return h ? h->tuning.c_str() : ""; }
 

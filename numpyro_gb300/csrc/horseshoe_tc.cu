@@ -412,6 +412,11 @@ void horseshoe_tc_free(ModelDev& m) {
   m.hs_tc = nullptr;
 }
 
+int* horseshoe_tc_error_ptr(const ModelDev& m) {
+  hstc::HsState* s = reinterpret_cast<hstc::HsState*>(m.hs_tc);
+  return s ? s->err : nullptr;
+}
+
 int horseshoe_tc_error(const ModelDev& m) {
   hstc::HsState* s = reinterpret_cast<hstc::HsState*>(m.hs_tc);
   if (!s) return 0;

@@ -88,6 +88,15 @@ void launch_init_state(const AdvParams* dP, int C, int D, const float* inv_mass_
 void launch_init_dense_mass(const AdvParams* dP, int C, const float* inv_mass_init, cudaStream_t st);
 void launch_set_phase(const AdvParams* dP, int C, int phase, int iters, cudaStream_t st);
 void launch_set_rng_chain(uint32_t* rng_key, int C, int first_chain, cudaStream_t st);
+// copies a parameter block (passed by value) into device memory, in stream order
+void launch_set_params(const AdvParams& p, AdvParams* dst, cudaStream_t st);
+// Last node of the device-side tick loop (a CUDA-graph WHILE node): counts the iteration in
+// iter[0] and keeps the loop going while a chain is active (counters[2 last + 1]), the budget
+// iter[1] is not exhausted and no tensor-core wait timed out; an active chain at the budget or a
+// timed-out wait sets *err_word to GBN_ERR_TIMEOUT.
+void launch_tick_condition(unsigned long long cond_handle, const int32_t* counters, int last, int32_t* iter,
+                           const int* tc_err, int32_t* err_word, cudaStream_t st);
+cudaError_t logreg_simt_smem_attr();
 
 // potentials_simt.cu: returns cudaError of the launch
 cudaError_t ensure_potential_scratch(ModelDev& m, int points);
@@ -108,6 +117,7 @@ bool horseshoe_tc_supported(const ModelDev& m);
 cudaError_t horseshoe_tc_prepare(ModelDev& m, int points);
 void horseshoe_tc_free(ModelDev& m);
 int horseshoe_tc_error(const ModelDev& m);  // nonzero: a device wait timed out
+int* horseshoe_tc_error_ptr(const ModelDev& m);  // device address of that error word (or null)
 cudaError_t horseshoe_tc_launch(ModelDev& m, const float* Q, int npts, double* PE, float* G, const int32_t* pending,
                                 cudaStream_t st);
 
@@ -116,6 +126,7 @@ bool logreg_tc_supported(const ModelDev& m);
 cudaError_t logreg_tc_prepare(ModelDev& m, int points);
 void logreg_tc_free(ModelDev& m);
 int logreg_tc_error(const ModelDev& m);  // nonzero: a device wait timed out
+int* logreg_tc_error_ptr(const ModelDev& m);  // device address of that error word (or null)
 cudaError_t logreg_tc_launch(ModelDev& m, const float* Q, int npts, double* PE, float* G, const int32_t* pending,
                              cudaStream_t st);
 

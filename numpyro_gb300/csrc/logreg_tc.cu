@@ -494,6 +494,11 @@ void logreg_tc_free(ModelDev& m) {
   m.tc = nullptr;
 }
 
+int* logreg_tc_error_ptr(const ModelDev& m) {
+  tc::TCState* s = reinterpret_cast<tc::TCState*>(m.tc);
+  return s ? s->err : nullptr;
+}
+
 int logreg_tc_error(const ModelDev& m) {
   tc::TCState* s = reinterpret_cast<tc::TCState*>(m.tc);
   if (!s) return 0;

@@ -1259,4 +1259,32 @@ void launch_set_rng_chain(uint32_t* rng_key, int C, int first_chain, cudaStream_
   set_rng_chain_kernel<<<(C + 255) / 256, 256, 0, st>>>(rng_key, C, first_chain);
 }
 
+__global__ void set_params_kernel(const AdvParams p, AdvParams* dst) {
+  static_assert(sizeof(AdvParams) % 16 == 0, "AdvParams is copied as 16-byte words");
+  const uint4* src = reinterpret_cast<const uint4*>(&p);
+  uint4* d = reinterpret_cast<uint4*>(dst);
+  for (int i = threadIdx.x; i < (int)(sizeof(AdvParams) / 16); i += blockDim.x) d[i] = src[i];
+}
+
+void launch_set_params(const AdvParams& p, AdvParams* dst, cudaStream_t st) {
+  set_params_kernel<<<1, 32, 0, st>>>(p, dst);
+}
+
+__global__ void tick_condition_kernel(cudaGraphConditionalHandle handle, const int32_t* counters, int last,
+                                      int32_t* iter, const int* tc_err, int32_t* err_word) {
+  const int it = iter[0] + 1;
+  iter[0] = it;
+  const bool active = counters[2 * last + 1] != 0;
+  const bool failed = tc_err != nullptr && *tc_err != 0;
+  const bool over = it >= iter[1];
+  if (active && (over || failed)) *err_word = 4;  // GBN_ERR_TIMEOUT
+  cudaGraphSetConditional(handle, (active && !over && !failed) ? 1u : 0u);
+}
+
+void launch_tick_condition(unsigned long long cond_handle, const int32_t* counters, int last, int32_t* iter,
+                           const int* tc_err, int32_t* err_word, cudaStream_t st) {
+  tick_condition_kernel<<<1, 1, 0, st>>>((cudaGraphConditionalHandle)cond_handle, counters, last, iter, tc_err,
+                                         err_word);
+}
+
 }  // namespace gbn

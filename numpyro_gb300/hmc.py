@@ -323,6 +323,19 @@ class HMC(MCMCKernel):
         _lib.check(lib.gbn_sample(self._handle, self._stream(), ctypes.byref(st)), self._handle)
         return new
 
+    def sample_async(self, state, model_args=(), model_kwargs={}):
+        """``sample`` enqueued on the current stream without any host synchronisation
+        (gbn_sample_async): the tick loop runs on the device.  Bit-identical to ``sample``;
+        ``check_async`` reports a tick budget exhausted on the device."""
+        new = self.copy_state(state)
+        st = self._cstate(new)
+        _lib.check(_lib.load().gbn_sample_async(self._handle, self._stream(), ctypes.byref(st)), self._handle)
+        return new
+
+    def check_async(self):
+        """Waits for the current stream and raises if an asynchronous transition failed on the device."""
+        _lib.check(_lib.load().gbn_check_async(self._handle, self._stream()), self._handle)
+
     def run_device(self, state, num_iterations, collect_start=0, thinning=1, collect=("z",)):
         """Runs ``num_iterations`` transitions per chain entirely on the device,
         updating ``state`` in place; returns a dict of collected [C, S, ...] tensors."""
