@@ -55,14 +55,17 @@ def parse():
     p.add_argument("--samples", type=int, default=None, help="sampling iterations of a --workload run")
     p.add_argument("--full-samples", type=int, default=1000,
                    help="sampling iterations of the full run (500 warmup + this) reported beside the timed steps")
-    p.add_argument("--oracle-samples", type=int, default=30,
+    p.add_argument("--oracle-samples", type=int, default=50,
                    help="transitions per chain of the FP64 oracle leg of the posterior check; 0 = skip")
+    p.add_argument("--diagnose", action="store_true",
+                   help="--workload uneven_hier / sv: also run numpyro's algorithm (FP64 C restatement) on "
+                        "the same chains and report its R-hat beside the GPU's")
     p.add_argument("--no-workloads", action="store_true",
                    help="skip the other benchmark configurations (eight schools, uneven hierarchical, horseshoe, SV)")
     return p.parse_args()
 
 
-def workload_run(w, precision=None, num_warmup=None, num_samples=None):
+def workload_run(w, precision=None, num_warmup=None, num_samples=None, diagnose=False):
     """Full NUTS run (warmup + sampling, both timed with CUDA events) of one of the other
     benchmark configurations at its shape; returns the figures of one JSON sub-object."""
     import torch
@@ -169,21 +172,72 @@ def workload_run(w, precision=None, num_warmup=None, num_samples=None):
         roof = {"bound": "tensor" if precision == "bf16x3" else "fp32", "achieved": tf, "peak": burst,
                 "unit": "TFLOP/s", "frac": tf / burst, "flop_per_grad_eval": 4.0 * N * P,
                 "peak_kind": peak_kind + " burst bf16"}
+    diag = None
+    if diagnose:
+        diag = _oracle_diagnosis(w, model, z, picked if w == "uneven_hier" else None, W, S, rhat if w == "uneven_hier"
+                                 else None)
     line = {"workload": w, "shape": shape, "chains": C, "num_warmup": W, "num_samples": S,
             "warmup_s": warm_s, "sampling_s": samp_s, "grad_evals_per_s_sampling": grad_evals / samp_s,
             "mean_num_steps": float(ns.mean()), "divergences": divergences,
             "min_bulk_ess": ess_min, "min_bulk_ess_per_s_sampling": ess_min / samp_s,
             "min_bulk_ess_per_s_total": ess_min / (warm_s + samp_s), "rhat_max": rhat_max,
-            "ess_definition": ess_note, "ticks_sampling": ticks, "us_per_tick": 1e6 * samp_s / max(1, ticks),
+            "ess_definition": ess_note, "ticks_sampling": ticks if ticks else None,
+            "us_per_tick": 1e6 * samp_s / ticks if ticks else None,
+            "engine": "tick engine + CUDA graphs" if ticks else "persistent (one launch)",
             "roofline": roof, "tuning": k.tuning()}
+    if diag is not None:
+        line["fp64_oracle_diagnosis"] = diag
     k.close()
     return line
+
+
+def _oracle_diagnosis(w, model, z, picked, W, S, model_rhat):
+    """Runs numpyro's algorithm (the FP64 C restatement, oracle/nuts_ref.c) on chains of the same
+    workload with the same chain ids and random stream as the GPU run, and reports its split
+    R-hat and divergences beside the GPU's on the same chains: whether the GPU's R-hat reflects
+    the sampler on this posterior or the engine."""
+    from oracle import build_oracle
+
+    lib = build_oracle.load("f64")
+    cores = len(os.sched_getaffinity(0))
+    cm = build_oracle.model_from_registry(model, 4)
+    out = {"oracle": "FP64 C restatement of numpyro's NUTS, same chain ids and Philox stream, %d warmup + "
+                     "%d samples, %d host threads" % (W, S, cores)}
+    if w == "uneven_hier":
+        order = np.argsort(model_rhat)[::-1][:4]  # the four models of the sample with the largest GPU R-hat
+        rows = []
+        for i in order:
+            m = picked[i]
+            D = model.chain_latent_dim(4 * m, 4)
+            res = build_oracle.run_model(lib, cm, model.latent_dim, 4, W, S, seed=1, first_chain=4 * m,
+                                         threads=min(cores, 4))
+            _, r_o = min_bulk_ess(res["samples"][:, :, :D])
+            e_o, _ = min_bulk_ess(res["samples"][:, :, :D])
+            e_g, r_g = min_bulk_ess(z[4 * i:4 * i + 4, :, :D])
+            rows.append({"model": int(m), "J": D - 2, "gpu_rhat": r_g, "oracle_rhat": r_o, "gpu_min_bulk_ess": e_g,
+                         "oracle_min_bulk_ess": e_o, "oracle_divergences": int(res["diverging"].sum())})
+        out["worst_models"] = rows
+        return out
+    if w in ("sv", "sv_nc"):
+        nc = min(16, cores)
+        T = model.latent_dim - 2
+        res = build_oracle.run_model(lib, cm, model.latent_dim, nc, W, S, seed=1, threads=nc)
+        idx = list(range(0, T, 16)) + [T, T + 1]
+        zo = res["samples"][:, :, idx]
+        e_o, r_o = min_bulk_ess(zo)
+        e_g, r_g = min_bulk_ess(z[:nc, :, :len(idx)])
+        out.update({"chains": nc, "gpu_rhat_same_chains": r_g, "oracle_rhat": r_o, "gpu_min_bulk_ess_same_chains": e_g,
+                    "oracle_min_bulk_ess": e_o, "oracle_divergences": int(res["diverging"].sum()),
+                    "oracle_s": [float(np.exp(zo[c, :, -1]).mean()) for c in range(nc)]})
+        return out
+    return None
 
 
 def run_workload(args):
     """--workload: one JSON line for one of the other benchmark configurations."""
     print(json.dumps(workload_run(args.workload, args.precision,
-                                  None if args.num_warmup == 500 else args.num_warmup, args.samples)))
+                                  None if args.num_warmup == 500 else args.num_warmup, args.samples,
+                                  diagnose=args.diagnose)))
     return 0
 
 
@@ -325,9 +379,9 @@ def oracle_moment_check(X, y, state, zgpu, chains, transitions):
     """The GPU posterior against the FP64 oracle's: the C oracle (FP64 build) runs ``chains``
     chains for ``transitions`` NUTS transitions from the GPU's adapted state, and each
     coefficient's posterior mean and sd are compared, in units of their Monte Carlo standard
-    error (sd / sqrt(bulk-ESS), combined over both samples; for the sd, sd / sqrt(2 ESS))."""
+    errors combined over both samples (diagnostics.mcse_mean, mcse_sd)."""
     from oracle import build_oracle
-    from numpyro_gb300.diagnostics import bulk_effective_sample_size
+    from numpyro_gb300.diagnostics import bulk_effective_sample_size, mcse_mean, mcse_sd
 
     lib = build_oracle.load("f64")
     cores = len(os.sched_getaffinity(0))
@@ -340,18 +394,13 @@ def oracle_moment_check(X, y, state, zgpu, chains, transitions):
     zg = np.asarray(zgpu, np.float64)
 
     def moments(z):
-        m = z.mean(axis=(0, 1))
-        sd = z.std(axis=(0, 1), ddof=1)
-        ess = np.concatenate([np.atleast_1d(bulk_effective_sample_size(z[..., d0:d0 + 64]))
-                              for d0 in range(0, z.shape[-1], 64)])
-        return m, sd, ess
+        return (z.mean(axis=(0, 1)), z.std(axis=(0, 1), ddof=1), mcse_mean(z), mcse_sd(z),
+                np.atleast_1d(bulk_effective_sample_size(z)))
 
-    mg, sg, eg = moments(zg)
-    mo, so, eo = moments(zo)
-    mcse_m = np.sqrt(sg ** 2 / eg + so ** 2 / eo)
-    mcse_s = np.sqrt(sg ** 2 / (2 * eg) + so ** 2 / (2 * eo))
-    zm = np.abs(mg - mo) / mcse_m
-    zs = np.abs(sg - so) / mcse_s
+    mg, sg, emg, esg, _ = moments(zg)
+    mo, so, emo, eso, eo = moments(zo)
+    zm = np.abs(mg - mo) / np.sqrt(emg ** 2 + emo ** 2)
+    zs = np.abs(sg - so) / np.sqrt(esg ** 2 + eso ** 2)
     return {"oracle": "FP64 C restatement of numpyro's NUTS, %d chains x %d transitions from the GPU's "
                       "adapted state (%.0f s on %d host threads)" % (chains, transitions, res["sampling_s"],
                                                                     res["threads"]),
@@ -523,6 +572,10 @@ def main():
                 "peak_kind": peak_kind + " burst bf16",
                 "kernel": "logreg potential (%s)" % precision, "algorithmic_flop_per_launch": flop,
                 "launch_ms": pot_ms}
+    if precision == "bf16x3":
+        # the binding pipe of the tensor-core potential: the special-function unit (ex2 + tanh per
+        # logit, one lg2 per 8 rows), against its own measured peak on this GPU
+        roofline["special_function_unit"] = _sfu_roofline(pot_ms, X.shape[0], C)
     # ---------------- end to end through the public API with host buffers
     e2e = None
     if not args.no_e2e:
@@ -612,6 +665,26 @@ def _tc_available():
         return bool(getattr(_lib.load(), "gbn_tc_available", lambda: 0)())
     except Exception:
         return False
+
+
+def _sfu_roofline(launch_ms, n, chains):
+    """Special-function operations of one tensor-core potential launch (2.125 per logit: one
+    ex2, one tanh, one lg2 per 8 rows) per second, against the unit's peak measured on this GPU
+    for the same mix (gbn_measure_sfu)."""
+    import torch
+
+    from numpyro_gb300 import _lib
+
+    peak = ctypes.c_double(0.0)
+    rc = _lib.load().gbn_measure_sfu(ctypes.c_void_p(torch.cuda.current_stream().cuda_stream), 2,
+                                     ctypes.byref(peak))
+    ops = 2.125 * n * chains
+    achieved = ops / (launch_ms * 1e-3)
+    if rc != 0 or peak.value <= 0:
+        return {"bound": "sfu", "achieved": achieved / 1e12, "peak": None, "unit": "Tops/s", "frac": None}
+    return {"bound": "sfu", "achieved": achieved / 1e12, "peak": peak.value / 1e12, "unit": "Tops/s",
+            "frac": achieved / peak.value, "ops_per_launch": ops, "ops_per_logit": 2.125,
+            "peak_kind": "measured in this run (gbn_measure_sfu: the epilogue's ex2/tanh/lg2 mix on every SM)"}
 
 
 def _launches_per_tick(precision):

@@ -208,6 +208,13 @@ int gbn_get_stats(gbn_handle h, gbn_stats* stats);
  * keeps the defaults.  No counterpart in the reference. */
 const char* gbn_tuning(gbn_handle h);
 
+/* Measurement utility, no counterpart in the reference: the peak throughput (operations per
+ * second, whole GPU) of the special-function unit on the operations of the tensor-core logistic
+ * epilogue -- mode 0 ex2.approx, 1 tanh.approx, 2 their mix in the epilogue's proportion (8 ex2,
+ * 8 tanh, 1 lg2) -- measured with independent dependency chains on every SM (a few ms).  The
+ * roofline of that kernel's special-function work is taken against it. */
+int gbn_measure_sfu(void* stream, int32_t mode, double* ops_per_second);
+
 /* Largest num_points accepted by gbn_logreg_potential_noalloc. */
 #define GBN_NOALLOC_MAX_POINTS 256
 

@@ -817,6 +817,13 @@ int gbn_check_async(gbn_handle h, void* stream) {
 
 const char* gbn_tuning(gbn_handle h) { return h ? h->tuning.c_str() : ""; }
 
+int gbn_measure_sfu(void* stream, int32_t mode, double* ops_per_second) {
+  if (!ops_per_second || mode < 0 || mode > 2) return fail(nullptr, GBN_ERR_INVALID_ARG, "gbn_measure_sfu: bad argument");
+  cudaError_t e = measure_sfu_rate(mode, (cudaStream_t)stream, ops_per_second);
+  if (e != cudaSuccess) return cuda_fail(nullptr, e, "gbn_measure_sfu");
+  return GBN_OK;
+}
+
 int gbn_get_stats(gbn_handle h, gbn_stats* stats) {
   if (!h || !stats) return fail(h, GBN_ERR_INVALID_ARG, "gbn_get_stats: null argument");
   *stats = h->stats;

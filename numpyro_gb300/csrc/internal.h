@@ -97,6 +97,8 @@ void launch_set_params(const AdvParams& p, AdvParams* dst, cudaStream_t st);
 void launch_tick_condition(unsigned long long cond_handle, const int32_t* counters, int last, int32_t* iter,
                            const int* tc_err, int32_t* err_word, cudaStream_t st);
 cudaError_t logreg_simt_smem_attr();
+// special-function unit throughput (operations/s) for mode 0 ex2, 1 tanh, 2 the logistic epilogue's mix
+cudaError_t measure_sfu_rate(int mode, cudaStream_t st, double* ops_per_s);
 
 // potentials_simt.cu: returns cudaError of the launch
 cudaError_t ensure_potential_scratch(ModelDev& m, int points);

@@ -695,6 +695,71 @@ cudaError_t autotune_potential(ModelDev& m, const float* Q, int npts, double* PE
   return cudaSuccess;
 }
 
+// ============================================================ special-function throughput
+// Peak rate of the special-function unit for the operations of the tensor-core logistic epilogue
+// (ex2.approx, tanh.approx, lg2.approx), measured with independent dependency chains (8 per
+// thread) so the unit, not latency, sets the rate.  MIX issues them in the epilogue's proportion:
+// per 16 operations 8 ex2 + 8 tanh, plus one lg2 (the epilogue's 2.125 per logit).
+template <int MODE>
+__global__ void __launch_bounds__(256) sfu_rate_kernel(int iters) {
+  float v[8];
+#pragma unroll
+  for (int k = 0; k < 8; ++k) v[k] = 0.25f + 0.01f * (float)(k + (threadIdx.x & 7));
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      float y;
+      if (MODE == 0 || (MODE == 2 && (k & 1) == 0))
+        asm volatile("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(-v[k]));
+      else
+        asm volatile("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(v[k]));
+      v[k] = y;
+    }
+    if (MODE == 2 && (i & 1)) {
+      float y;
+      asm volatile("lg2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(1.0f + v[0]));
+      v[0] = 0.5f * y;
+    }
+  }
+  float acc = 0.0f;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) acc += v[k];
+  asm volatile("" ::"f"(acc));  // a use of every chain, so none is dead code
+}
+
+cudaError_t measure_sfu_rate(int mode, cudaStream_t st, double* ops_per_s) {
+  int dev = 0, sms = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (e != cudaSuccess) return e;
+  const int blocks = sms * 8, threads = 256, iters = 4096;
+  cudaEvent_t a = nullptr, b = nullptr;
+  e = cudaEventCreate(&a);
+  if (e == cudaSuccess) e = cudaEventCreate(&b);
+  auto launch = [&]() {
+    if (mode == 0) sfu_rate_kernel<0><<<blocks, threads, 0, st>>>(iters);
+    else if (mode == 1) sfu_rate_kernel<1><<<blocks, threads, 0, st>>>(iters);
+    else sfu_rate_kernel<2><<<blocks, threads, 0, st>>>(iters);
+  };
+  if (e == cudaSuccess) {
+    launch();  // warm-up
+    e = cudaEventRecord(a, st);
+  }
+  const int reps = 5;
+  for (int r = 0; r < reps && e == cudaSuccess; ++r) launch();
+  if (e == cudaSuccess) e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaEventRecord(b, st);
+  if (e == cudaSuccess) e = cudaEventSynchronize(b);
+  float ms = 0.0f;
+  if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, a, b);
+  // operations per launch: 8 chains x iters per thread, plus the mix's lg2 every other iteration
+  const double per_thread = 8.0 * iters + (mode == 2 ? iters / 2 : 0);
+  if (e == cudaSuccess) *ops_per_s = per_thread * blocks * threads * reps / (ms * 1e-3);
+  if (a) cudaEventDestroy(a);
+  if (b) cudaEventDestroy(b);
+  return e;
+}
+
 cudaError_t launch_scale_rows(const double* cot, float* G, int npts, int D, cudaStream_t st) {
   size_t total = (size_t)npts * D;
   int blocks = (int)((total + 255) / 256);

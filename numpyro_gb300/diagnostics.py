@@ -99,6 +99,28 @@ def effective_sample_size(x, bias=True):
     return np.prod(x.shape[:2]) / tau
 
 
+def mcse_mean(x):
+    """Monte Carlo standard error of the posterior mean of each coordinate of x [C, S, ...]:
+    sd / sqrt(ESS), with numpyro's effective_sample_size."""
+    x = np.asarray(x, np.float64)
+    sd = x.reshape((-1,) + x.shape[2:]).std(axis=0, ddof=1)
+    return sd / np.sqrt(effective_sample_size(x))
+
+
+def mcse_sd(x):
+    """Monte Carlo standard error of the posterior sd of each coordinate of x [C, S, ...]: the
+    delta method on the variance, whose own error is that of the mean of the squared deviations
+    (their ESS, not the draws' -- NUTS draws are often antithetic for x but not for x^2):
+    mcse(sd) = sqrt(var(d^2) / ESS(d^2)) / (2 sd), d = x - mean (Vehtari et al. 2021, sec. 3)."""
+    x = np.asarray(x, np.float64)
+    flat = x.reshape((-1,) + x.shape[2:])
+    m = flat.mean(axis=0)
+    sd = flat.std(axis=0, ddof=1)
+    d2 = (x - m) ** 2
+    var_d2 = d2.reshape((-1,) + x.shape[2:]).var(axis=0, ddof=1)
+    return np.sqrt(var_d2 / effective_sample_size(d2)) / (2.0 * sd)
+
+
 def _split_chains(x):
     n_half = x.shape[1] // 2
     return np.concatenate([x[:, :n_half], x[:, -n_half:]], axis=0)

@@ -122,6 +122,27 @@ class Model:
         return ctypes.byref(self.struct)
 
 
+def model_from_registry(model, chains_per_model=1):
+    """The C restatement's copy of a numpyro_gb300 registry model, read from its public
+    attributes (datasets / X, y / returns and the family's options)."""
+    kind = type(model).__name__
+    if kind == "HierarchicalNormal":
+        y = np.concatenate([a for a, _ in model.datasets])
+        s = np.concatenate([b for _, b in model.datasets])
+        off = np.zeros(len(model.datasets) + 1, np.int32)
+        off[1:] = np.cumsum([len(a) for a, _ in model.datasets])
+        return Model("hier_nc", y=y, sigma=s, offsets=off, chains_per_model=chains_per_model,
+                     hyper=(model.mu_scale, model.tau_scale))
+    if kind == "LogisticRegression":
+        return Model("logreg", X=model.X, y=model.y, hyper=(model.prior_scale,))
+    if kind == "HorseshoeRegression":
+        return Model("horseshoe_nc" if model.noncentered else "horseshoe", X=model.X, y=model.y)
+    if kind == "StochasticVolatility":
+        return Model("sv_nc" if model.noncentered else "sv", y=model.returns,
+                     hyper=(model.s_rate, model.nu_rate, 1.0 if model.noncentered else 0.0))
+    raise TypeError("no C restatement of %s" % kind)
+
+
 def potential(lib, model, z, model_index=0):
     """(U, dU/dz) of one point, from the C restatement (FP64 with the f64 build)."""
     z = np.ascontiguousarray(z, np.float64)

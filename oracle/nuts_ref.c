@@ -141,7 +141,10 @@ static double digamma_ref(double x) {
  *        2 (s + s^3/3 + ... + s^13/13) (Abramowitz & Stegun 4.1.28; truncation error < 2e-8). */
 static inline float exp_neg_f(float x) { /* e^x for x <= 0 */
   x = x < -87.0f ? -87.0f : x;
-  const float kf = (x * 1.44269504088896341f + 12582912.0f) - 12582912.0f;
+  /* k = round(x log2 e): x <= 0, so truncating x log2 e - 1/2 toward zero rounds to nearest
+   * (the build reassociates float sums, so an add-and-subtract rounding trick would fold away) */
+  const int32_t ki = (int32_t)(x * 1.44269504088896341f - 0.5f);
+  const float kf = (float)ki;
   const float r = (x - kf * 0.693145751953125f) - kf * 1.428606765330187e-06f;
   float p = 1.0f / 720.0f;
   p = p * r + 1.0f / 120.0f;
@@ -151,7 +154,7 @@ static inline float exp_neg_f(float x) { /* e^x for x <= 0 */
   p = p * r + 1.0f;
   p = p * r + 1.0f;
   union { float f; int32_t i; } u;
-  u.i = ((int32_t)kf + 127) << 23;
+  u.i = (ki + 127) << 23;
   return p * u.f;
 }
 static inline float log1p_unit_f(float t) { /* log(1 + t) for t in [0, 1] */

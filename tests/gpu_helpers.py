@@ -118,18 +118,4 @@ def cmodel_of(model, chains_per_model=1):
     """The C oracle's copy of a registry model (oracle/nuts_ref.c nutsref_model)."""
     from oracle import build_oracle as B
 
-    if isinstance(model, models.HierarchicalNormal):
-        y = np.concatenate([a for a, _ in model.datasets])
-        s = np.concatenate([b for _, b in model.datasets])
-        off = np.zeros(model.num_models + 1, np.int32)
-        off[1:] = np.cumsum(model.J)
-        return B.Model("hier_nc", y=y, sigma=s, offsets=off, chains_per_model=chains_per_model,
-                       hyper=(model.mu_scale, model.tau_scale))
-    if isinstance(model, models.LogisticRegression):
-        return B.Model("logreg", X=model.X, y=model.y, hyper=(model.prior_scale,))
-    if isinstance(model, models.HorseshoeRegression):
-        return B.Model("horseshoe_nc" if model.noncentered else "horseshoe", X=model.X, y=model.y)
-    if isinstance(model, models.StochasticVolatility):
-        return B.Model("sv_nc" if model.noncentered else "sv", y=model.returns,
-                       hyper=(model.s_rate, model.nu_rate, 1.0 if model.noncentered else 0.0))
-    raise TypeError(model)
+    return B.model_from_registry(model, chains_per_model)

@@ -56,3 +56,14 @@ def test_summary_keys_and_values():
     assert 0.99 < float(s["a"]["r_hat"]) < 1.01
     flat = summary({"a": rng.normal(size=(2000,))}, group_by_chain=False)
     assert flat["a"]["n_eff"] > 1000
+
+
+def test_mcse_of_mean_and_sd_on_independent_normal_draws():
+    """Known answers: for independent N(0, 1) draws the standard errors of the mean and of the sd
+    are 1 / sqrt(N) and 1 / sqrt(2 N)."""
+    from numpyro_gb300.diagnostics import mcse_mean, mcse_sd
+
+    x = np.random.default_rng(0).standard_normal((8, 2000, 4))
+    n = 8 * 2000
+    np.testing.assert_allclose(mcse_mean(x), 1 / np.sqrt(n), rtol=0.1)
+    np.testing.assert_allclose(mcse_sd(x), 1 / np.sqrt(2 * n), rtol=0.1)

@@ -1,0 +1,107 @@
+"""Posterior gates at reduced sizes of the benchmark configurations, against the FP64 oracle.
+
+The benchmark's correctness criterion: split R-hat (numpyro/diagnostics.py:64-80) < 1.01 for
+every coordinate, and every posterior mean and sd within 3 Monte Carlo standard errors of the
+FP64 oracle's (the Monte Carlo standard errors of both samples combined in quadrature:
+numpyro_gb300.diagnostics.mcse_mean and mcse_sd, the latter from the ESS of the squared
+deviations).  The oracle is the FP64 C restatement of numpyro's NUTS (oracle/nuts_ref.c),
+run on the host cores: with its own Stan warmup from init_to_uniform where that is cheap, or,
+for the logistic model, from the GPU's adapted state (its first draws are discarded, so a GPU
+posterior that were off would show as the oracle chains drifting away from it).
+
+Sizes: logistic 20,000 rows x 55 coefficients (FP32 CUDA cores and bf16x3 tensor cores),
+stochastic volatility T = 512, non-centred horseshoe N = 200, P = 50 (FP32 and bf16x3), and
+8 uneven hierarchical datasets (J from 4 to 64) in one launch.
+"""
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+
+from numpyro_gb300 import NUTS, datasets, models  # noqa: E402
+from numpyro_gb300.diagnostics import (bulk_effective_sample_size, mcse_mean, mcse_sd,  # noqa: E402
+                                       split_gelman_rubin)
+from oracle import build_oracle as B  # noqa: E402
+
+from gpu_helpers import cmodel_of  # noqa: E402
+
+SEED = 11
+
+
+def _stats(z):
+    z = np.asarray(z, np.float64)
+    m = z.mean(axis=(0, 1))
+    sd = z.std(axis=(0, 1), ddof=1)
+    ess = np.atleast_1d(bulk_effective_sample_size(z))
+    rhat = np.atleast_1d(split_gelman_rubin(z))
+    return m, sd, mcse_mean(z), mcse_sd(z), ess, rhat
+
+
+def _gate(name, zg, zo, rhat_max=1.01, thr=3.0):
+    mg, sg, emg, esg, eg, rg = _stats(zg)
+    mo, so, emo, eso, eo, ro = _stats(zo)
+    zm = np.abs(mg - mo) / np.sqrt(emg ** 2 + emo ** 2)
+    zs = np.abs(sg - so) / np.sqrt(esg ** 2 + eso ** 2)
+    print("%s: GPU R-hat max %.4f (oracle %.4f), min bulk-ESS GPU %.0f oracle %.0f; "
+          "max |dmean|/MCSE %.2f, max |dsd|/MCSE %.2f over %d coordinates"
+          % (name, rg.max(), ro.max(), eg.min(), eo.min(), zm.max(), zs.max(), zm.size))
+    assert rg.max() < rhat_max, (name, rg.max())
+    assert zm.max() <= thr, (name, int(np.argmax(zm)), zm.max())
+    assert zs.max() <= thr, (name, int(np.argmax(zs)), zs.max())
+
+
+def _gpu_run(model, C, W, S, **kw):
+    k = NUTS(model, num_chains=C, **kw)
+    st = k.init(SEED, W)
+    k.run_device(st, W, collect_start=W, collect=())
+    z = k.run_device(st, S, collect=("z",))["z"].cpu().numpy()
+    k.close()
+    return z, st
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", ["fp32", "bf16x3"])
+def test_logistic_posterior_gate(precision):
+    X, y, _ = datasets.covtype_like(seed=5, n=20_000)
+    model = models.LogisticRegression(X, y)
+    zg, st = _gpu_run(model, 256, 300, 300, precision=precision)
+    nc = 16
+    init = (st.z[:nc].cpu().numpy(), st.adapt_state.step_size[:nc].cpu().numpy(),
+            st.adapt_state.inverse_mass_matrix[:nc].cpu().numpy())
+    res = B.run_model(B.load("f64"), cmodel_of(model), X.shape[1], nc, 0, 350, seed=SEED + 1, init=init)
+    _gate("logistic N=20000 %s" % precision, zg, res["samples"][:, 50:])
+
+
+@pytest.mark.gpu
+def test_stochastic_volatility_posterior_gate():
+    r, _ = datasets.sv_returns(seed=0, T=512)
+    model = models.StochasticVolatility(r)
+    zg, _ = _gpu_run(model, 64, 1000, 1000)
+    res = B.run_model(B.load("f64"), cmodel_of(model), model.latent_dim, 16, 1000, 1000, seed=SEED + 2)
+    _gate("sv T=512", zg, res["samples"])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", ["fp32", "bf16x3"])
+def test_horseshoe_posterior_gate(precision):
+    X, y, _ = datasets.horseshoe_data(seed=3, n=200, p=50, nonzero=5)
+    model = models.HorseshoeRegression(X, y, noncentered=True)
+    zg, _ = _gpu_run(model, 128, 1000, 1000, precision=precision)
+    res = B.run_model(B.load("f64"), cmodel_of(model), model.latent_dim, 16, 1000, 1000, seed=SEED + 3)
+    _gate("horseshoe_nc N=200 P=50 %s" % precision, zg, res["samples"])
+
+
+@pytest.mark.gpu
+def test_uneven_hierarchical_posterior_gate():
+    ds = datasets.uneven_hierarchical(seed=4, num_models=8, jmin=4, jmax=64)
+    model = models.HierarchicalNormal(datasets=ds)
+    cpm = 16
+    zg, _ = _gpu_run(model, cpm * len(ds), 1000, 1000)
+    cm = cmodel_of(model, chains_per_model=cpm)
+    lib = B.load("f64")
+    for k, (yk, _) in enumerate(ds):
+        D = len(yk) + 2
+        # the oracle's chains of dataset k: global chain ids k * cpm .. k * cpm + 7
+        res = B.run_model(lib, cm, model.latent_dim, 8, 1000, 1000, seed=SEED + 4, first_chain=k * cpm)
+        _gate("uneven hierarchical dataset %d (J=%d)" % (k, len(yk)), zg[k * cpm:(k + 1) * cpm, :, :D],
+              res["samples"][:, :, :D])

@@ -86,14 +86,17 @@ def _run_across(k, st, pot, until, steps, C, **kw):
                 ok = False
                 break
             assert a.window_idx == g["widx"][c], (c, s, a.window_idx, g["widx"][c])
-            np.testing.assert_allclose(g["step"][c], a.step_size, rtol=2e-4, err_msg="chain %d step %d" % (c, s))
+            # dual averaging turns an accept-probability difference da into a relative step-size
+            # difference of sqrt(t) / (gamma (t + t0)) da, 1.8 da at t = 1 just after a window end;
+            # FP32 accept probabilities agree with FP64 to ~1e-3, hence 2e-3
+            np.testing.assert_allclose(g["step"][c], a.step_size, rtol=2e-3, err_msg="chain %d step %d" % (c, s))
             np.testing.assert_allclose(g["inv"][c], a.inverse_mass_matrix, rtol=1e-4, atol=1e-7,
                                        err_msg="chain %d step %d" % (c, s))
             np.testing.assert_allclose(g["msq"][c], a.mass_matrix_sqrt, rtol=1e-4,
                                        err_msg="chain %d step %d" % (c, s))
             assert g["n"][c] == a.mm_state[2], (c, s)
             # the prox centre log(10 step) carries the step size's relative error as an absolute one
-            np.testing.assert_allclose(g["ss"][c][4], a.ss_state[4], rtol=0, atol=2e-4)
+            np.testing.assert_allclose(g["ss"][c][4], a.ss_state[4], rtol=0, atol=2e-3)
         agree += ok
     return agree, cur
 

@@ -149,3 +149,27 @@ def test_c_transitions_match_python_restatement(lib64):
             assert bool(st.diverging) == bool(out["diverging"][c]), (name, c)
             assert abs(st.accept_prob - out["accept_prob"][c]) < 1e-7, (name, c)
             np.testing.assert_allclose(out["z"][c], st.z, rtol=2e-6, atol=1e-6, err_msg="%s %d" % (name, c))
+
+
+def test_f32_build_potentials_match_f64():
+    """The FP32 build (numpyro's float32 dtype; the timed CPU baseline, with its own vectorisable
+    exp and log1p for the logistic rows) agrees with the FP64 build to FP32 rounding."""
+    from gpu_helpers import typical_points
+
+    lib32, lib64 = B.load("f32"), B.load("f64")
+    rng = np.random.default_rng(3)
+    X, yy, beta = datasets.covtype_like(seed=0, n=20000)
+    m = B.Model("logreg", X=X, y=yy)
+    for sc in (0.01, 1.0, 5.0):
+        z = beta + sc * rng.standard_normal(beta.shape)
+        p64, g64 = B.potential(lib64, m, z)
+        p32, g32 = B.potential(lib32, m, z)
+        assert abs(p32 - p64) <= 1e-6 * abs(p64), (sc, p32, p64)
+        assert np.max(np.abs(g32 - g64)) <= 1e-5 * np.max(np.abs(g64)), sc
+    for name, mm, _, D, _ in _family_cases():
+        z = typical_points(name, _Dim(D), rng, 2).astype(np.float64)
+        for c in range(2):
+            p64, g64 = B.potential(lib64, mm, z[c])
+            p32, g32 = B.potential(lib32, mm, z[c])
+            assert abs(p32 - p64) <= 1e-5 * abs(p64) + 1e-4, (name, p32, p64)
+            assert np.max(np.abs(g32 - g64)) <= 1e-4 * np.max(np.abs(g64)) + 1e-4, name
