@@ -204,19 +204,29 @@ def _oracle_diagnosis(w, model, z, picked, W, S, model_rhat):
     out = {"oracle": "FP64 C restatement of numpyro's NUTS, same chain ids and Philox stream, %d warmup + "
                      "%d samples, %d host threads" % (W, S, cores)}
     if w == "uneven_hier":
-        order = np.argsort(model_rhat)[::-1][:4]  # the four models of the sample with the largest GPU R-hat
-        rows = []
-        for i in order:
-            m = picked[i]
+        # every model of the strided sample, 4 chains each with the GPU's chain ids and stream: the
+        # distribution of per-model R-hat and ESS under numpyro's algorithm beside the GPU's
+        g_r, g_e, o_r, o_e, o_div, rows = [], [], [], [], 0, []
+        for i, m in enumerate(picked):
             D = model.chain_latent_dim(4 * m, 4)
             res = build_oracle.run_model(lib, cm, model.latent_dim, 4, W, S, seed=1, first_chain=4 * m,
                                          threads=min(cores, 4))
-            _, r_o = min_bulk_ess(res["samples"][:, :, :D])
-            e_o, _ = min_bulk_ess(res["samples"][:, :, :D])
+            e_o, r_o = min_bulk_ess(res["samples"][:, :, :D])
             e_g, r_g = min_bulk_ess(z[4 * i:4 * i + 4, :, :D])
+            g_r.append(r_g), g_e.append(e_g), o_r.append(r_o), o_e.append(e_o)
+            o_div += int(res["diverging"].sum())
             rows.append({"model": int(m), "J": D - 2, "gpu_rhat": r_g, "oracle_rhat": r_o, "gpu_min_bulk_ess": e_g,
                          "oracle_min_bulk_ess": e_o, "oracle_divergences": int(res["diverging"].sum())})
-        out["worst_models"] = rows
+        g_r, o_r, g_e, o_e = map(np.asarray, (g_r, o_r, g_e, o_e))
+        out.update({"models": len(picked),
+                    "gpu_models_rhat_over_1.01": int(np.sum(g_r > 1.01)),
+                    "oracle_models_rhat_over_1.01": int(np.sum(o_r > 1.01)),
+                    "gpu_models_rhat_over_1.05": int(np.sum(g_r > 1.05)),
+                    "oracle_models_rhat_over_1.05": int(np.sum(o_r > 1.05)),
+                    "gpu_rhat_max": float(g_r.max()), "oracle_rhat_max": float(o_r.max()),
+                    "gpu_median_min_bulk_ess": float(np.median(g_e)), "oracle_median_min_bulk_ess": float(np.median(o_e)),
+                    "oracle_divergences": o_div,
+                    "worst_models": sorted(rows, key=lambda r: -max(r["gpu_rhat"], r["oracle_rhat"]))[:6]})
         return out
     if w in ("sv", "sv_nc"):
         nc = min(16, cores)
