@@ -67,3 +67,24 @@ def test_mcse_of_mean_and_sd_on_independent_normal_draws():
     n = 8 * 2000
     np.testing.assert_allclose(mcse_mean(x), 1 / np.sqrt(n), rtol=0.1)
     np.testing.assert_allclose(mcse_sd(x), 1 / np.sqrt(2 * n), rtol=0.1)
+
+
+def test_posterior_gate_bounds():
+    """The chance allowance of the posterior gates (tests/test_gpu_posterior_gates.py): independent
+    standard-normal z-scores pass it about 99 % of the time."""
+    import importlib.util
+    import os
+
+    pytest.importorskip("torch")
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "test_gpu_posterior_gates.py")
+    spec = importlib.util.spec_from_file_location("gates_under_test", path)
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    b3, bound = mod.moment_bounds(110)
+    assert b3 == 2 and abs(bound - 3.91) < 0.01
+    b3, bound = mod.moment_bounds(1028)
+    assert b3 == 8 and abs(bound - 4.42) < 0.01
+    z = np.abs(np.random.default_rng(1).standard_normal((2000, 110)))
+    b3, bound = mod.moment_bounds(110)
+    ok = (np.sum(z > 3, axis=1) <= b3) & (z.max(axis=1) <= bound)
+    assert ok.mean() > 0.97
