@@ -413,16 +413,20 @@ __global__ void __launch_bounds__(256) horseshoe_finish_kernel(const float* __re
   g.sum2ff(flp, fgt, red);
   FF frr = g.sumff(rr_ff, red);
   if (tid == 0) {
+    // The scalar factors come from FP32 transcendentals (correctly rounded to ~1 ulp) and are
+    // combined in FP64 where a term is large (N log sigma, RR / sigma^2): an FP64 exp or log1p on
+    // one thread costs microseconds on GB300's FP64 pipe, at the end of every chain's launch.
     const double RR = ff_value(frr), dlsig = lsig, dltau = ltau;
-    const double sig = exp(dlsig), tau = exp(dltau), inv_s2 = exp(-2.0 * dlsig);
+    const float sigf = expf(lsig), tauf = expf(ltau);
+    const double sig = sigf, tau = tauf, inv_s2 = inv_sig2;
     // per coordinate: Normal(beta; 0, tau lambda) or Normal(unscaled; 0, 1), HalfCauchy(lambda; 1)
     double total = ff_value(flp) + (double)P * (LOG_2 - LOG_PI - 0.5 * LOG_2PI - (noncentred ? 0.0 : dltau));
     total += -0.5 * sig * sig - 0.5 * LOG_2PI + LOG_2 + dlsig;  // HalfNormal(sigma; 1) + log-det
-    total += -LOG_PI - log1p(tau * tau) + LOG_2 + dltau;        // HalfCauchy(tau; 1) + log-det
+    total += -LOG_PI - (double)log1pf(tauf * tauf) + LOG_2 + dltau;  // HalfCauchy(tau; 1) + log-det
     total += -0.5 * RR * inv_s2 - (double)N * dlsig - 0.5 * (double)N * LOG_2PI;
     PE[c] = -total;
     gz[i_sig] = (float)(sig * sig - 1.0 - RR * inv_s2 + (double)N);
-    gz[i_tau] = (float)(ff_value(fgt) + 2.0 * tau * tau / (1.0 + tau * tau) - 1.0);
+    gz[i_tau] = (float)(ff_value(fgt) + (double)(2.0f * tauf * tauf / (1.0f + tauf * tauf)) - 1.0);
   }
 }
 
