@@ -76,7 +76,7 @@ class NutsrefModel(ctypes.Structure):
     _fields_ = [("family", ctypes.c_int32), ("num_models", ctypes.c_int32), ("chains_per_model", ctypes.c_int32),
                 ("P", ctypes.c_int32), ("N", ctypes.c_int64), ("X", ctypes.c_void_p), ("y", ctypes.c_void_p),
                 ("sigma", ctypes.c_void_p), ("offsets", ctypes.c_void_p), ("hyper", ctypes.c_double * 4),
-                ("row_threads", ctypes.c_int32)]
+                ("row_threads", ctypes.c_int32), ("target_accept", ctypes.c_double)]
 
 
 class Model:
@@ -84,7 +84,7 @@ class Model:
     horseshoe_nc, sv, sv_nc (as oracle.potentials_ref.FAMILIES)."""
 
     def __init__(self, kind, X=None, y=None, sigma=None, offsets=None, chains_per_model=1, hyper=None,
-                 row_threads=0):
+                 row_threads=0, target_accept=0.8):
         fam = {"hier_nc": 1, "logreg": 2, "horseshoe": 3, "horseshoe_nc": 3, "sv": 4, "sv_nc": 4}[kind]
         self.kind = kind
         self.X = None if X is None else np.ascontiguousarray(X, np.float32)
@@ -116,6 +116,7 @@ class Model:
         s.offsets = _p(self.offsets)
         s.hyper = (ctypes.c_double * 4)(*h)
         s.row_threads = int(row_threads)
+        s.target_accept = float(target_accept)
         self.struct = s
 
     def ref(self):

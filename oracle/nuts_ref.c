@@ -97,6 +97,7 @@ typedef struct {
   const int32_t* offsets;
   double hyper[4];
   int32_t row_threads; /* logistic family: threads sharing one chain's rows (0/1: none) */
+  double target_accept; /* dual-averaging target accept probability (0: numpyro's default 0.8) */
 } nutsref_model;
 
 int nutsref_latent_dim(const nutsref_model* m, int model_index) {
@@ -437,7 +438,7 @@ typedef struct {
   int D, maxd, k; /* latent dim, checkpoint rows, dataset index */
   real *z, *g, *inv, *msq;
   real *zl, *rl, *gl, *zr, *rr, *gr, *zp, *gp, *zsp, *gsp, *rs, *rss, *rck, *sck, *tmp;
-  double pe, step, ss[5];
+  double pe, step, ss[5], target_accept;
   double *mean, *m2;
   int mm_n, window_idx;
   long grad_evals;
@@ -598,7 +599,7 @@ static void adapt(chain_t* c, int t, double accept_prob, int num_warmup, const i
   double* ss = c->ss;
   ss[3] += 1.0;
   double tt = ss[3];
-  ss[2] = (1 - 1 / (tt + 10)) * ss[2] + (0.8 - accept_prob) / (tt + 10);
+  ss[2] = (1 - 1 / (tt + 10)) * ss[2] + (c->target_accept - accept_prob) / (tt + 10);
   ss[0] = ss[4] - pow(tt, 0.5) / 0.05 * ss[2];
   double wt = pow(tt, -0.75);
   ss[1] = (1 - wt) * ss[1] + wt * ss[0];
@@ -727,6 +728,7 @@ int nutsref_run_model(const nutsref_model* m, int ld, int chains, int first_chai
       c->step = 1.0;
     }
     c->ss[4] = log(10.0 * c->step);
+    c->target_accept = m->target_accept > 0 ? m->target_accept : 0.8;
   }
   tw0 = now_s();
 #pragma omp parallel for schedule(dynamic, 1) reduction(+ : gw) if (m->row_threads <= 1)
