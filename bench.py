@@ -698,9 +698,12 @@ def _sfu_roofline(launch_ms, n, chains):
 
 
 def _launches_per_tick(precision):
-    # advance_kernel, then the potential: split_coefs + logreg_tc + logreg_finish on the tensor
-    # cores, logreg_simt + logreg_finish on CUDA cores (the launch list in profiles/ shows the four)
-    return 4 if precision == "bf16x3" else 3
+    # advance_kernel, then the potential: on the tensor cores the tcgen05 kernel alone (the
+    # coefficient split and the row-group finish run inside advance_kernel; GBN_FUSE_TICK=0 launches
+    # them separately, 4 per tick), on CUDA cores logreg_simt + logreg_finish
+    if precision == "bf16x3":
+        return 4 if os.environ.get("GBN_FUSE_TICK", "1") == "0" else 2
+    return 3
 
 
 def _time_potential(kernel, state, reps=10, batch=20):

@@ -58,7 +58,23 @@ struct gbn_handle_s {
   // gbn_sample_async: a graph whose WHILE node repeats tick batches until no chain is active
   cudaGraphExec_t async_graph = nullptr;
   int32_t* async_iter = nullptr;  // [2]: loop iterations done, iteration budget
+  void* async_scratch = nullptr;  // potential scratch the async graph was built with
+  int fuse_tick = 1;              // GBN_FUSE_TICK=0: the tensor-core logistic potential runs unfused
 };
+
+// The tick engine fuses the tensor-core logistic potential's coefficient split and row-group finish
+// into its advance kernel; the pointers (which a larger gbn_potential_and_grad call may reallocate)
+// are refreshed before every upload of the parameter block.
+static void refresh_fusion(gbn_handle h) {
+  AdvParams& P = h->hp;
+  P.lrf_part_g = nullptr;
+  P.lrf_part_ll = nullptr;
+  P.lrf_lin = nullptr;
+  P.lrf_bsplit = nullptr;
+  if (h->fuse_tick && !h->persistent && h->m.family == GBN_FAMILY_LOGREG && h->m.precision == GBN_PREC_BF16X3 &&
+      h->m.tc && !logreg_tc_fusion(h->m, h->C, &P))
+    P.lrf_part_g = nullptr;
+}
 
 static thread_local std::string g_last_error;
 
@@ -387,6 +403,8 @@ int gbn_create(gbn_handle* out, const gbn_model_desc* md, const gbn_config* cfg)
   {
     const char* g = getenv("GBN_CUDA_GRAPHS");  // "0" launches every tick directly
     h->use_graphs = !(g && g[0] == '0');
+    const char* f = getenv("GBN_FUSE_TICK");  // "0": the tensor-core logistic potential's split and finish
+    h->fuse_tick = !(f && f[0] == '0');       // run as their own kernels
   }
   if (ce == cudaSuccess && m.family == GBN_FAMILY_LOGREG && m.precision == GBN_PREC_BF16X3) {
     if (!logreg_tc_supported(m)) {
@@ -452,6 +470,7 @@ int gbn_create(gbn_handle* out, const gbn_model_desc* md, const gbn_config* cfg)
   P.counters = h->counters;
   P.error_word = h->err_word;
   P.thinning = 1;
+  refresh_fusion(h);
   {
     std::lock_guard<std::mutex> lock(g_handles_mu);
     h->id = g_next_id++;
@@ -505,7 +524,8 @@ static cudaError_t launch_tick_batch(gbn_handle h, cudaStream_t st) {
   for (int k = 0; k < TICK_BATCH; ++k) {
     const int parity = k & 1;
     launch_advance(h->dP, h->C, h->D, h->cta_per_chain, h->hp.dense != 0, parity, st);
-    cudaError_t e = launch_potential(h->m, h->e.Q, h->C, h->e.PE, h->e.G, h->counters + 2 * parity, st);
+    cudaError_t e = launch_potential(h->m, h->e.Q, h->C, h->e.PE, h->e.G, h->counters + 2 * parity, st,
+                                     h->hp.lrf_part_g != nullptr);
     if (e != cudaSuccess) return e;
   }
   return cudaSuccess;
@@ -594,6 +614,7 @@ int gbn_init(gbn_handle h, void* stream, int32_t num_warmup, const float* d_init
   P.num_collect = 0;
   P.collect_start = 0;
   P.thinning = 1;
+  refresh_fusion(h);
   e = upload_params(h, s);
   if (e != cudaSuccess) return cuda_fail(h, e, "gbn_init: params");
   launch_set_rng_chain(st->rng_key, h->C, 0, s);
@@ -676,6 +697,7 @@ int gbn_run(gbn_handle h, void* stream, gbn_state* st, int32_t num_iterations, i
     h->done_cap = num_iterations + 1;
   }
   P.done_count = h->done_count;
+  refresh_fusion(h);
   e = upload_params(h, s);
   if (e == cudaSuccess) e = cudaMemsetAsync(h->done_count, 0, sizeof(int32_t) * (num_iterations + 1), s);
   if (e == cudaSuccess) e = cudaMemsetAsync(h->counters, 0, sizeof(int32_t) * 4, s);
@@ -764,7 +786,13 @@ int gbn_sample_async(gbn_handle h, void* stream, gbn_state* st) {
   P.thinning = 1;
   P.num_collect = 0;
   P.done_count = h->done_count;  // sized for one transition at gbn_create
+  refresh_fusion(h);
   cudaError_t e = cudaSuccess;
+  void* scratch = h->m.part_g ? (void*)h->m.part_g : (void*)h->m.resid;
+  if (h->async_graph && h->async_scratch != scratch) {  // scratch was reallocated since the build
+    cudaGraphExecDestroy(h->async_graph);
+    h->async_graph = nullptr;
+  }
   if (!h->persistent && !h->async_graph) {  // first call of the handle: build the tick-loop graph
     int64_t per_iter = (h->cfg.algo == GBN_ALGO_HMC) ? 4096 : ((int64_t)1 << h->maxd) + 8;
     if (h->cfg.find_heuristic_step_size) per_iter += 512;
@@ -773,6 +801,7 @@ int gbn_sample_async(gbn_handle h, void* stream, gbn_state* st) {
     e = cudaMemcpy(h->async_iter, budget, sizeof(budget), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = build_async_graph(h);
     if (e != cudaSuccess) return cuda_fail(h, e, "gbn_sample_async: graph set-up");
+    h->async_scratch = scratch;
   }
   launch_set_params(P, h->dP, s);
   e = cudaMemsetAsync(h->done_count, 0, sizeof(int32_t) * 2, s);

@@ -273,6 +273,16 @@ struct __align__(16) AdvParams {
   int32_t* counters;    // [4]: (pending, active) for parity 0 and 1
   int32_t* done_count;  // lock-step barrier counts, [max iterations + 1]
   int32_t* error_word;  // device error status
+  // The tensor-core logistic potential fused into the tick engine (lrf_part_g null: not fused):
+  // the advance kernel finishes the previous tick's potential from its row-group partials
+  // (logreg_finish_warp) and writes the bf16x3 coefficient splits of every position it queries.
+  const float* lrf_part_g;
+  const double* lrf_part_ll;
+  const double* lrf_lin;
+  uint16_t* lrf_bsplit;  // [chains, padded][3][64] bfloat16 bits
+  double lrf_pe_const;
+  float lrf_inv_var;
+  int32_t lrf_row_groups;
 };
 
 // ---------------------------------------------------------------- groups

@@ -103,8 +103,10 @@ cudaError_t measure_sfu_rate(int mode, cudaStream_t st, double* ops_per_s);
 // potentials_simt.cu: returns cudaError of the launch
 cudaError_t ensure_potential_scratch(ModelDev& m, int points);
 void free_potential_scratch(ModelDev& m);
+// fused_tick: the tick engine's call, whose advance kernel fuses the tensor-core logistic
+// potential's coefficient split and finish (logreg_tc_fusion); other potentials ignore it
 cudaError_t launch_potential(ModelDev& m, const float* Q, int npts, double* PE, float* G,
-                             const int32_t* pending, cudaStream_t st);
+                             const int32_t* pending, cudaStream_t st, bool fused_tick = false);
 // Times the candidate launch shapes of this model's potential at npts points (Q: any valid
 // [npts][D] positions; PE/G outputs) and stores the fastest in m.tune.  Decisions are cached per
 // process for each (device, family, shape, points), so every handle of a shape runs the same
@@ -130,6 +132,9 @@ void logreg_tc_free(ModelDev& m);
 int logreg_tc_error(const ModelDev& m);  // nonzero: a device wait timed out
 int* logreg_tc_error_ptr(const ModelDev& m);  // device address of that error word (or null)
 cudaError_t logreg_tc_launch(ModelDev& m, const float* Q, int npts, double* PE, float* G, const int32_t* pending,
-                             cudaStream_t st);
+                             cudaStream_t st, bool fused_tick = false);
+// Fills P's lrf_* fields so the tick engine's advance kernel fuses this potential's coefficient split
+// and row-group finish (launches over npts points); false when the tensor-core path is not set up.
+bool logreg_tc_fusion(const ModelDev& m, int npts, AdvParams* P);
 
 }  // namespace gbn

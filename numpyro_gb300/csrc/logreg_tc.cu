@@ -511,22 +511,48 @@ void logreg_finish_launch(const float* Q, int npts, int ld, int p, int row_group
                           const double* part_ll, const double* lin, double prior_scale, double* PE, float* G,
                           const int32_t* pending, cudaStream_t st);
 
+// row groups of a launch over npts points: the grid fills the SMs with (chain blocks x row groups)
+static int logreg_tc_row_groups(const ModelDev& m, int npts) {
+  const int blocks = (npts + tc::BN - 1) / tc::BN;
+  const int64_t ntiles = (m.n + tc::BM - 1) / tc::BM;
+  int rg = std::max(1, 152 / blocks);
+  if (rg > ntiles) rg = (int)ntiles;
+  if (rg > m.row_groups) rg = m.row_groups;  // partial buffers are sized for m.row_groups
+  return rg;
+}
+
+void logreg_prior_consts(double prior_scale, int p, float* inv_var_f, double* pe_const);
+
+bool logreg_tc_fusion(const ModelDev& m, int npts, AdvParams* P) {
+  tc::TCState* s = reinterpret_cast<tc::TCState*>(m.tc);
+  if (!s || !s->ok || !s->bsplit || !m.part_g) return false;
+  P->lrf_part_g = m.part_g;
+  P->lrf_part_ll = m.part_ll;
+  P->lrf_lin = s->lin;
+  P->lrf_bsplit = reinterpret_cast<uint16_t*>(s->bsplit);
+  P->lrf_row_groups = logreg_tc_row_groups(m, npts);
+  logreg_prior_consts(m.hyper[0], m.p, &P->lrf_inv_var, &P->lrf_pe_const);
+  return true;
+}
+
 cudaError_t logreg_tc_launch(ModelDev& m, const float* Q, int npts, double* PE, float* G, const int32_t* pending,
-                             cudaStream_t st) {
+                             cudaStream_t st, bool fused_tick) {
   tc::TCState* s = reinterpret_cast<tc::TCState*>(m.tc);
   if (!s || !s->ok) return cudaErrorNotSupported;
   cudaError_t e = logreg_tc_prepare(m, npts);
   if (e != cudaSuccess) return e;
-  int blocks = (npts + tc::BN - 1) / tc::BN;
-  int64_t ntiles = (m.n + tc::BM - 1) / tc::BM;
-  int rg = std::max(1, 152 / blocks);
-  if (rg > ntiles) rg = (int)ntiles;
-  if (rg > m.row_groups) rg = m.row_groups;  // partial buffers are sized for m.row_groups
-  int npad = blocks * tc::BN;
-  tc::split_coefs_kernel<<<(npad * tc::BK + 255) / 256, 256, 0, st>>>(Q, npts, m.D, m.p, npad, s->bsplit, pending);
+  const int blocks = (npts + tc::BN - 1) / tc::BN;
+  const int rg = logreg_tc_row_groups(m, npts);
+  const int npad = blocks * tc::BN;
+  // In the tick engine's fused form the state-machine kernel writes the coefficient splits with
+  // the positions and finishes the sums, so only the tensor-core kernel runs here.
+  if (!fused_tick)
+    tc::split_coefs_kernel<<<(npad * tc::BK + 255) / 256, 256, 0, st>>>(Q, npts, m.D, m.p, npad, s->bsplit,
+                                                                         pending);
   tc::Params P{m.n, s->bsplit, npts, rg, m.part_g, m.part_ll, s->err, pending};
   tc::logreg_tc_kernel<<<dim3(blocks, rg), tc::NUM_THREADS, tc::SMEM_BYTES, st>>>(s->tmap, P);
-  logreg_finish_launch(Q, npts, m.D, m.p, rg, m.part_g, m.part_ll, s->lin, m.hyper[0], PE, G, pending, st);
+  if (!fused_tick)
+    logreg_finish_launch(Q, npts, m.D, m.p, rg, m.part_g, m.part_ll, s->lin, m.hyper[0], PE, G, pending, st);
   return cudaGetLastError();
 }
 

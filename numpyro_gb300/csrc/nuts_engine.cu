@@ -24,9 +24,12 @@
 //   warmup_adapter.update_fn :637-705, find_reasonable_step_size :314-384;
 // numpyro/infer/hmc.py: momentum_generator :92-110, _hmc_next :364-414,
 //   _nuts_next :416-455, sample_kernel :459-530.
+#include <cuda_bf16.h>
+
 #include "common.cuh"
 #include "hier_potential.cuh"
 #include "internal.h"
+#include "lr_finish.cuh"
 #include "sv_potential.cuh"
 
 namespace gbn {
@@ -110,6 +113,24 @@ struct Chain {
   __device__ __forceinline__ float* G_() const { return V(P.e.G); }
 
   __device__ __forceinline__ size_t row() const { return (size_t)c * ld; }
+
+  // q[d] = v for the potential; when the tensor-core logistic potential is fused into the tick,
+  // also the exact hi/mid/lo bfloat16 terms of v / 2 that its GEMM reads (as split_coefs_kernel)
+  __device__ __forceinline__ void put_q(float* q, int d, float v) const {
+    q[d] = v;
+    if (P.lrf_bsplit) {
+      const float h = 0.5f * v;
+      const __nv_bfloat16 hi = __float2bfloat16_rn(h);
+      const float r1 = h - __bfloat162float(hi);
+      const __nv_bfloat16 mid = __float2bfloat16_rn(r1);
+      const float r2 = r1 - __bfloat162float(mid);
+      const __nv_bfloat16 lo = __float2bfloat16_rn(r2);
+      uint16_t* o = P.lrf_bsplit + (size_t)c * 192 + d;
+      o[0] = __bfloat16_as_ushort(hi);
+      o[64] = __bfloat16_as_ushort(mid);
+      o[128] = __bfloat16_as_ushort(lo);
+    }
+  }
   __device__ __forceinline__ float* V(float* base) const { return base + row(); }
   __device__ __forceinline__ float* CK(float* base, int k) const { return base + ((size_t)c * P.maxd + k) * ld; }
 
@@ -257,7 +278,7 @@ struct Chain {
       sym_matvec(MX(P.s.inverse_mass_matrix), r, [&](int d, float v) {
         const float zn = z[d] + eps * v;
         z[d] = zn;
-        q[d] = zn;
+        put_q(q, d, zn);
       });
       return;
     }
@@ -280,7 +301,7 @@ struct Chain {
         float zn = zz[k] + eps * (mm[k] * rh);
         r[d] = rh;
         z[d] = zn;
-        q[d] = zn;
+        put_q(q, d, zn);
       }
     }
   }
@@ -706,7 +727,7 @@ struct Chain {
         rh[d] = v - 0.5f * eps * gz[d];
       });
       const double k0 = kinetic_dense(r0);  // synchronises after r0 and rh were written
-      sym_matvec(MX(P.s.inverse_mass_matrix), rh, [&](int d, float v) { q[d] = z[d] + eps * v; });
+      sym_matvec(MX(P.s.inverse_mass_matrix), rh, [&](int d, float v) { put_q(q, d, z[d] + eps * v); });
       ctl.heur_e0 = P.s.potential_energy[c] + k0;
       ctl.phase = PH_HEUR;
       return;
@@ -719,7 +740,7 @@ struct Chain {
       r0[d] = r;
       float h = r - 0.5f * eps * gz[d];
       rh[d] = h;
-      q[d] = z[d] + eps * (mi[d] * h);
+      put_q(q, d, z[d] + eps * (mi[d] * h));
     }
     ctl.heur_e0 = P.s.potential_energy[c] + 0.5 * ff_value(g.sumff(ff_from(kin), red));
     ctl.phase = PH_HEUR;
@@ -959,6 +980,14 @@ __global__ void __launch_bounds__(256) advance_kernel(const AdvParams* __restric
     P.counters[2 * (parity ^ 1) + 1] = 0;
   }
   int pending = 0, active = 0;
+  if (NT == 32 && P.lrf_part_g && c < P.C) {
+    // the tensor-core logistic potential of the previous tick ends here for the chains that queried it
+    const int ph = P.e.ctl[c].phase;
+    if (ph == PH_LEAF || ph == PH_HMC || ph == PH_HEUR)
+      logreg_finish_warp(P.e.Q, c, P.C, P.D, P.D, P.lrf_row_groups, P.lrf_part_g, P.lrf_part_ll, P.lrf_lin,
+                         P.lrf_inv_var, P.lrf_pe_const, P.e.PE, P.e.G, tid);
+    __syncwarp();  // G and PE written by other lanes
+  }
   if (c < P.C) {
     Chain<NT, DM> ch{P, Group<NT>{tid}, red, c, P.e.chain_dim ? P.e.chain_dim[c] : P.D, P.D, P.e.ctl[c], nullptr};
     ch.run();

@@ -19,9 +19,12 @@
 #include <mutex>
 #include <string>
 #include <vector>
+#include <cmath>
+
 #include "common.cuh"
 #include "hier_potential.cuh"
 #include "internal.h"
+#include "lr_finish.cuh"
 #include "sv_potential.cuh"
 
 namespace gbn {
@@ -179,46 +182,19 @@ __global__ void __launch_bounds__(256) logreg_simt_kernel(const float* __restric
 // lin (optional, FP64 [p]): a linear term lin . b of the log-likelihood computed outside the kernel
 __global__ void logreg_finish_kernel(const float* __restrict__ Q, int npts, int ld, int p, int row_groups,
                                      const float* __restrict__ part_g, const double* __restrict__ part_ll,
-                                     const double* __restrict__ lin, double prior_scale, double* __restrict__ PE,
-                                     float* __restrict__ G, const int32_t* pending) {
+                                     const double* __restrict__ lin, float inv_var_f, double pe_const,
+                                     double* __restrict__ PE, float* __restrict__ G, const int32_t* pending) {
   if (pending && *pending == 0) return;
-  int c = blockIdx.x * 8 + (threadIdx.x >> 5);
-  int lane = threadIdx.x & 31;
+  const int c = blockIdx.x * 8 + (threadIdx.x >> 5);
   if (c >= npts) return;
-  const float inv_var_f = (float)(1.0 / (prior_scale * prior_scale));
-  const double inv_var = (double)inv_var_f;
-  double lp = 0.0;
-  for (int d = lane; d < p; d += 32) {
-    const float bf = Q[(size_t)c * ld + d];
-    // the row groups' FP32 gradient partials are summed in FP32 (the gradient is FP32); the
-    // potential's prior and linear terms stay FP64 (lin . b reaches ~1e5 on large data)
-    // (loads issued 8 at a time ahead of the in-order sum: the same sum, without a serialised
-    // memory latency per row group)
-    float s = 0.0f;
-    const float* pg = part_g + (size_t)c * 64 + d;
-    const size_t rs = (size_t)npts * 64;
-    int r = 0;
-    for (; r + 8 <= row_groups; r += 8) {
-      float t[8];
-#pragma unroll
-      for (int k = 0; k < 8; ++k) t[k] = pg[(size_t)(r + k) * rs];
-#pragma unroll
-      for (int k = 0; k < 8; ++k) s += t[k];
-    }
-    for (; r < row_groups; ++r) s += pg[(size_t)r * rs];
-    G[(size_t)c * ld + d] = fmaf(bf, inv_var_f, s);
-    const double b = (double)bf;
-    lp += 0.5 * b * b * inv_var;
-    if (lin) lp += lin[d] * b;
-  }
-  double ll = 0.0;
-  for (int r = lane; r < row_groups; r += 32) ll += part_ll[(size_t)r * npts + c];
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    lp += __shfl_xor_sync(0xffffffffu, lp, o);
-    ll += __shfl_xor_sync(0xffffffffu, ll, o);
-  }
-  if (lane == 0) PE[c] = ll + lp + (double)p * (0.5 * LOG_2PI + log(prior_scale));
+  logreg_finish_warp(Q, c, npts, ld, p, row_groups, part_g, part_ll, lin, inv_var_f, pe_const, PE, G,
+                     threadIdx.x & 31);
+}
+
+// 1 / s^2 (FP32, as the gradient uses it) and p (log(2 pi) / 2 + log s) of the Normal(0, s) prior
+void logreg_prior_consts(double prior_scale, int p, float* inv_var_f, double* pe_const) {
+  *inv_var_f = (float)(1.0 / (prior_scale * prior_scale));
+  *pe_const = (double)p * (0.5 * LOG_2PI + std::log(prior_scale));
 }
 
 // ============================================================ horseshoe: FP32 GEMMs + prior terms
@@ -530,7 +506,7 @@ cudaError_t logreg_simt_smem_attr() {
 }
 
 cudaError_t launch_potential(ModelDev& m, const float* Q, int npts, double* PE, float* G, const int32_t* pending,
-                             cudaStream_t st) {
+                             cudaStream_t st, bool fused_tick) {
   if (npts <= 0) return cudaSuccess;
   cudaError_t e = ensure_potential_scratch(m, npts);
   if (e != cudaSuccess) return e;
@@ -545,7 +521,7 @@ cudaError_t launch_potential(ModelDev& m, const float* Q, int npts, double* PE, 
     }
       break;
     case 2: {
-      if (m.precision == 1 && m.tc) return logreg_tc_launch(m, Q, npts, PE, G, pending, st);
+      if (m.precision == 1 && m.tc) return logreg_tc_launch(m, Q, npts, PE, G, pending, st, fused_tick);
       int DP = logreg_dp(m.p);
       size_t sm = logreg_smem(DP);
       e = logreg_simt_smem_attr();
@@ -554,8 +530,11 @@ cudaError_t launch_potential(ModelDev& m, const float* Q, int npts, double* PE, 
       dim3 grid((npts + LR_CT - 1) / LR_CT, rg);
       logreg_simt_kernel<<<grid, 256, sm, st>>>(m.x, m.y, m.n, m.p, DP, Q, npts, ld, m.part_g, m.part_ll, rg,
                                                 pending);
-      logreg_finish_kernel<<<(npts + 7) / 8, 256, 0, st>>>(Q, npts, ld, m.p, rg, m.part_g, m.part_ll, nullptr,
-                                                           m.hyper[0], PE, G, pending);
+      float ivf;
+      double pec;
+      logreg_prior_consts(m.hyper[0], m.p, &ivf, &pec);
+      logreg_finish_kernel<<<(npts + 7) / 8, 256, 0, st>>>(Q, npts, ld, m.p, rg, m.part_g, m.part_ll, nullptr, ivf,
+                                                           pec, PE, G, pending);
       break;
     }
     case 3: {
@@ -789,8 +768,11 @@ cudaError_t launch_logreg_simt_scratch(const float* x, const float* y, int64_t n
                                                          nullptr);
   e = cudaGetLastError();  // checked per launch, so the first failing launch is the one reported
   if (e != cudaSuccess) return e;
-  logreg_finish_kernel<<<(npts + 7) / 8, 256, 0, st>>>(Q, npts, p, p, row_groups, part_g, part_ll, nullptr,
-                                                       prior_scale, PE, G, nullptr);
+  float ivf;
+  double pec;
+  logreg_prior_consts(prior_scale, p, &ivf, &pec);
+  logreg_finish_kernel<<<(npts + 7) / 8, 256, 0, st>>>(Q, npts, p, p, row_groups, part_g, part_ll, nullptr, ivf, pec,
+                                                       PE, G, nullptr);
   return cudaGetLastError();
 }
 
@@ -804,7 +786,10 @@ void horseshoe_finish_launch(const float* Q, int npts, int ld, int P, int64_t N,
 void logreg_finish_launch(const float* Q, int npts, int ld, int p, int row_groups, const float* part_g,
                           const double* part_ll, const double* lin, double prior_scale, double* PE, float* G,
                           const int32_t* pending, cudaStream_t st) {
-  logreg_finish_kernel<<<(npts + 7) / 8, 256, 0, st>>>(Q, npts, ld, p, row_groups, part_g, part_ll, lin,
-                                                       prior_scale, PE, G, pending);
+  float ivf;
+  double pec;
+  logreg_prior_consts(prior_scale, p, &ivf, &pec);
+  logreg_finish_kernel<<<(npts + 7) / 8, 256, 0, st>>>(Q, npts, ld, p, row_groups, part_g, part_ll, lin, ivf, pec, PE,
+                                                       G, pending);
 }
 }  // namespace gbn

@@ -51,5 +51,5 @@ def test_clock_sampler_without_nvidia_smi(monkeypatch):
 
 def test_launches_per_tick():
     b = _bench()
-    assert b._launches_per_tick("bf16x3") == 4  # advance, coefficient split, tensor-core potential, finish
+    assert b._launches_per_tick("bf16x3") == 2  # advance (with split and finish fused), tensor-core potential
     assert b._launches_per_tick("fp32") == 3    # advance, CUDA-core potential, finish

@@ -217,3 +217,28 @@ def test_tick_graph_replay_matches_direct_launches(family, monkeypatch):
         k.close()
     np.testing.assert_array_equal(res[0][0], res[1][0])
     np.testing.assert_array_equal(res[0][1], res[1][1])
+
+
+@pytest.mark.gpu
+def test_fused_tensor_core_tick_matches_separate_split_and_finish(monkeypatch):
+    """The tick engine folds the tensor-core logistic potential's coefficient split and row-group
+    finish into its state-machine kernel (two launches per tick instead of four); with
+    GBN_FUSE_TICK=0 they run as their own kernels.  Both forms share the arithmetic, so the draws
+    and tree sizes agree bit for bit, through warmup and sampling, and through the device-side
+    loop of gbn_sample_async."""
+    X, yv, _ = datasets.covtype_like(seed=6, n=20_000)
+    model = models.LogisticRegression(X, yv)
+    res = []
+    for fuse in ("1", "0"):
+        monkeypatch.setenv("GBN_FUSE_TICK", fuse)
+        k = NUTS(model, num_chains=256, precision="bf16x3")
+        st = k.init(SEED, 60)
+        out = k.run_device(st, 100, collect_start=0, collect=("z", "num_steps"))
+        for _ in range(3):
+            st = k.sample_async(st)
+        k.check_async()
+        res.append((out["z"].cpu().numpy(), out["num_steps"].cpu().numpy(), st.z.cpu().numpy(),
+                     st.potential_energy.cpu().numpy()))
+        k.close()
+    for a, b in zip(res[0], res[1]):
+        np.testing.assert_array_equal(a, b)
