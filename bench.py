@@ -565,7 +565,7 @@ def main():
     value = ess / (total_ms / 1e3)
     # ---------------- dominant kernel: the potential, timed alone on the same stream
     log("timed steps done: %.1f ms/step" % (total_ms / max(1, args.steps)))
-    pot_ms = _time_potential(kernel, state, reps=10)
+    pot_ms = _time_tick_potential(kernel, reps=10)
     burst, sustained, hbm, peak_kind = measured_peaks()
     flop = 4.0 * X.shape[0] * X.shape[1] * C
     achieved = flop / (pot_ms / 1e3) / 1e12
@@ -580,8 +580,10 @@ def main():
                 "frac": achieved / burst, "traffic": traffic, "traffic_unit": "bytes per launch",
                 "traffic_source": traffic_src,
                 "peak_kind": peak_kind + " burst bf16",
-                "kernel": "logreg potential (%s)" % precision, "algorithmic_flop_per_launch": flop,
-                "launch_ms": pot_ms}
+                "kernel": ("logreg_tc_kernel (bf16x3; coefficient split and row-group finish fused into the "
+                           "state-machine kernel)" if precision == "bf16x3" else
+                           "logreg potential (fp32: logreg_simt_kernel + logreg_finish_kernel)"),
+                "algorithmic_flop_per_launch": flop, "launch_ms": pot_ms}
     if precision == "bf16x3":
         # the binding pipe of the tensor-core potential: the special-function unit (ex2 + tanh per
         # logit, one lg2 per 8 rows), against its own measured peak on this GPU
@@ -724,6 +726,24 @@ def _time_potential(kernel, state, reps=10, batch=20):
         b.record()
         b.synchronize()
         ts.append(a.elapsed_time(b) / batch)
+    return float(np.median(ts))
+
+
+def _time_tick_potential(kernel, reps=10, batch=20):
+    """Duration of one potential launch as the tick engine issues it (for the tensor-core path the
+    tcgen05 kernel alone; gbn_time_potential), from CUDA events around ``batch`` back-to-back
+    launches on the current stream; median over ``reps`` batches."""
+    import torch
+
+    from numpyro_gb300 import _lib
+
+    lib = _lib.load()
+    stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    ts = []
+    for _ in range(reps):
+        v = ctypes.c_float(0.0)
+        _lib.check(lib.gbn_time_potential(kernel._handle, stream, batch, ctypes.byref(v)), kernel._handle)
+        ts.append(v.value)
     return float(np.median(ts))
 
 

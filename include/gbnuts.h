@@ -208,6 +208,12 @@ int gbn_get_stats(gbn_handle h, gbn_stats* stats);
  * keeps the defaults.  No counterpart in the reference. */
 const char* gbn_tuning(gbn_handle h);
 
+/* Measurement utility, no counterpart in the reference: the mean CUDA-event time (ms) of `reps`
+ * back-to-back launches of the handle's potential over all its chains, at their last query
+ * positions, in the form the tick engine launches it (for the tensor-core logistic potential the
+ * tcgen05 kernel alone: its coefficient split and finish run inside the state-machine kernel).
+ * Call it between runs, not during one. */
+int gbn_time_potential(gbn_handle h, void* stream, int32_t reps, float* ms);
 /* Measurement utility, no counterpart in the reference: the peak throughput (operations per
  * second, whole GPU) of the special-function unit on the operations of the tensor-core logistic
  * epilogue -- mode 0 ex2.approx, 1 tanh.approx, 2 their mix in the epilogue's proportion (8 ex2,

@@ -846,6 +846,30 @@ int gbn_check_async(gbn_handle h, void* stream) {
 
 const char* gbn_tuning(gbn_handle h) { return h ? h->tuning.c_str() : ""; }
 
+int gbn_time_potential(gbn_handle h, void* stream, int32_t reps, float* ms) {
+  if (!h || !ms || reps < 1) return fail(h, GBN_ERR_INVALID_ARG, "gbn_time_potential: bad argument");
+  cudaStream_t s = (cudaStream_t)stream;
+  refresh_fusion(h);
+  const bool fused = h->hp.lrf_part_g != nullptr;
+  cudaEvent_t a = nullptr, b = nullptr;
+  cudaError_t e = cudaEventCreate(&a);
+  if (e == cudaSuccess) e = cudaEventCreate(&b);
+  // the chains' last query positions; the engine's G and PE are rewritten before they are read again
+  if (e == cudaSuccess) e = launch_potential(h->m, h->e.Q, h->C, h->e.PE, h->e.G, nullptr, s, fused);
+  if (e == cudaSuccess) e = cudaEventRecord(a, s);
+  for (int r = 0; r < reps && e == cudaSuccess; ++r)
+    e = launch_potential(h->m, h->e.Q, h->C, h->e.PE, h->e.G, nullptr, s, fused);
+  if (e == cudaSuccess) e = cudaEventRecord(b, s);
+  if (e == cudaSuccess) e = cudaEventSynchronize(b);
+  float t = 0.0f;
+  if (e == cudaSuccess) e = cudaEventElapsedTime(&t, a, b);
+  if (a) cudaEventDestroy(a);
+  if (b) cudaEventDestroy(b);
+  if (e != cudaSuccess) return cuda_fail(h, e, "gbn_time_potential");
+  *ms = t / (float)reps;
+  return GBN_OK;
+}
+
 int gbn_measure_sfu(void* stream, int32_t mode, double* ops_per_second) {
   if (!ops_per_second || mode < 0 || mode > 2) return fail(nullptr, GBN_ERR_INVALID_ARG, "gbn_measure_sfu: bad argument");
   cudaError_t e = measure_sfu_rate(mode, (cudaStream_t)stream, ops_per_second);

@@ -684,7 +684,7 @@ cudaError_t autotune_potential(ModelDev& m, const float* Q, int npts, double* PE
 // thread) so the unit, not latency, sets the rate.  MIX issues them in the epilogue's proportion:
 // per 16 operations 8 ex2 + 8 tanh, plus one lg2 (the epilogue's 2.125 per logit).
 template <int MODE>
-__global__ void __launch_bounds__(256) sfu_rate_kernel(int iters) {
+__global__ void __launch_bounds__(256) sfu_rate_kernel(int iters, float* __restrict__ out) {
   float v[8];
 #pragma unroll
   for (int k = 0; k < 8; ++k) v[k] = 0.25f + 0.01f * (float)(k + (threadIdx.x & 7));
@@ -707,7 +707,7 @@ __global__ void __launch_bounds__(256) sfu_rate_kernel(int iters) {
   float acc = 0.0f;
 #pragma unroll
   for (int k = 0; k < 8; ++k) acc += v[k];
-  asm volatile("" ::"f"(acc));  // a use of every chain, so none is dead code
+  out[(size_t)blockIdx.x * blockDim.x + threadIdx.x] = acc;  // every chain's result is stored
 }
 
 cudaError_t measure_sfu_rate(int mode, cudaStream_t st, double* ops_per_s) {
@@ -717,12 +717,14 @@ cudaError_t measure_sfu_rate(int mode, cudaStream_t st, double* ops_per_s) {
   if (e != cudaSuccess) return e;
   const int blocks = sms * 8, threads = 256, iters = 4096;
   cudaEvent_t a = nullptr, b = nullptr;
-  e = cudaEventCreate(&a);
+  float* out = nullptr;  // one float per thread: the chains' results, so none is dead code
+  e = cudaMalloc(&out, sizeof(float) * (size_t)blocks * threads);
+  if (e == cudaSuccess) e = cudaEventCreate(&a);
   if (e == cudaSuccess) e = cudaEventCreate(&b);
   auto launch = [&]() {
-    if (mode == 0) sfu_rate_kernel<0><<<blocks, threads, 0, st>>>(iters);
-    else if (mode == 1) sfu_rate_kernel<1><<<blocks, threads, 0, st>>>(iters);
-    else sfu_rate_kernel<2><<<blocks, threads, 0, st>>>(iters);
+    if (mode == 0) sfu_rate_kernel<0><<<blocks, threads, 0, st>>>(iters, out);
+    else if (mode == 1) sfu_rate_kernel<1><<<blocks, threads, 0, st>>>(iters, out);
+    else sfu_rate_kernel<2><<<blocks, threads, 0, st>>>(iters, out);
   };
   if (e == cudaSuccess) {
     launch();  // warm-up
@@ -740,6 +742,7 @@ cudaError_t measure_sfu_rate(int mode, cudaStream_t st, double* ops_per_s) {
   if (e == cudaSuccess) *ops_per_s = per_thread * blocks * threads * reps / (ms * 1e-3);
   if (a) cudaEventDestroy(a);
   if (b) cudaEventDestroy(b);
+  if (out) cudaFree(out);
   return e;
 }
 
