@@ -51,18 +51,23 @@ def moment_bounds(n):
     return int(np.floor(n * p3 + 3 * np.sqrt(n * p3 * (1 - p3)) + 1)), float(norm.isf(0.005 / n))
 
 
-def _gate(name, zg, zo, rhat_max=1.01):
+def _gate(name, zg, zo, rhat_max=1.01, max_unconverged=0.0):
+    """R-hat of the GPU chains below rhat_max; the moments of every coordinate that both samples
+    have converged on (split R-hat < 1.01: a Monte Carlo standard error means nothing otherwise)
+    within what chance allows; at most max_unconverged of the coordinates left out."""
     mg, sg, emg, esg, eg, rg = _stats(zg)
     mo, so, emo, eso, eo, ro = _stats(zo)
-    zm = np.abs(mg - mo) / np.sqrt(emg ** 2 + emo ** 2)
-    zs = np.abs(sg - so) / np.sqrt(esg ** 2 + eso ** 2)
+    conv = (rg < 1.01) & (ro < 1.01)
+    zm = (np.abs(mg - mo) / np.sqrt(emg ** 2 + emo ** 2))[conv]
+    zs = (np.abs(sg - so) / np.sqrt(esg ** 2 + eso ** 2))[conv]
     z = np.concatenate([zm, zs])
     beyond3, bound = moment_bounds(z.size)
     print("%s: GPU R-hat max %.4f (oracle %.4f), min bulk-ESS GPU %.0f oracle %.0f; "
-          "max |dmean|/MCSE %.2f, max |dsd|/MCSE %.2f over %d coordinates; %d of %d comparisons beyond 3 MCSE "
-          "(chance allows %d), all within %.2f"
-          % (name, rg.max(), ro.max(), eg.min(), eo.min(), zm.max(), zs.max(), zm.size, np.sum(z > 3), z.size,
-             beyond3, bound))
+          "max |dmean|/MCSE %.2f, max |dsd|/MCSE %.2f over %d converged coordinates (of %d); %d of %d comparisons "
+          "beyond 3 MCSE (chance allows %d), all within %.2f"
+          % (name, rg.max(), ro.max(), eg.min(), eo.min(), zm.max(), zs.max(), zm.size, conv.size, np.sum(z > 3),
+             z.size, beyond3, bound))
+    assert np.mean(~conv) <= max_unconverged, (name, int(np.sum(~conv)))
     assert rg.max() < rhat_max, (name, rg.max())
     assert np.sum(z > 3.0) <= beyond3, (name, int(np.sum(z > 3.0)))
     assert z.max() <= bound, (name, int(np.argmax(z)), z.max())
@@ -108,7 +113,8 @@ def test_stochastic_volatility_posterior_gate():
 # four seeds (6.9-9.3 % of its transitions divergent; the half-Cauchy local scales of the null
 # coefficients leave funnels that some chains cross rarely).  So the GPU's R-hat is held to the
 # reference sampler's own range on the same posterior, chains and draws, and its divergence rate to
-# within half and one and a half times the oracle's.
+# within half and one and a half times the oracle's.  The moments are compared on the coordinates
+# both samples have converged on (at most a quarter may be left out).
 HORSESHOE_RHAT_OF_REFERENCE = 1.12
 
 
@@ -119,7 +125,8 @@ def test_horseshoe_posterior_gate(precision):
     model = models.HorseshoeRegression(X, y, noncentered=True)
     zg, _, dg = _gpu_run(model, 128, 1000, 3000, with_divergences=True, precision=precision)
     res = B.run_model(B.load("f64"), cmodel_of(model), model.latent_dim, 16, 1000, 3000, seed=SEED + 3)
-    _gate("horseshoe_nc N=200 P=50 %s" % precision, zg, res["samples"], rhat_max=HORSESHOE_RHAT_OF_REFERENCE)
+    _gate("horseshoe_nc N=200 P=50 %s" % precision, zg, res["samples"], rhat_max=HORSESHOE_RHAT_OF_REFERENCE,
+          max_unconverged=0.25)
     fg, fo = dg.mean(), res["diverging"].mean()
     print("divergent transitions: GPU %.4f, oracle %.4f" % (fg, fo))
     assert 0.5 * fo <= fg <= 1.5 * fo, (fg, fo)
