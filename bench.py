@@ -55,8 +55,9 @@ def parse():
     p.add_argument("--samples", type=int, default=None, help="sampling iterations of a --workload run")
     p.add_argument("--full-samples", type=int, default=1000,
                    help="sampling iterations of the full run (500 warmup + this) reported beside the timed steps")
-    p.add_argument("--oracle-samples", type=int, default=50,
-                   help="transitions per chain of the FP64 oracle leg of the posterior check; 0 = skip")
+    p.add_argument("--oracle-samples", type=int, default=200,
+                   help="transitions per chain of the FP64 oracle leg of the posterior check; 0 = skip "
+                        "(with 50 the oracle's short chains understate their own Monte Carlo error)")
     p.add_argument("--diagnose", action="store_true",
                    help="--workload uneven_hier / sv: also run numpyro's algorithm (FP64 C restatement) on "
                         "the same chains and report its R-hat beside the GPU's")
@@ -411,12 +412,20 @@ def oracle_moment_check(X, y, state, zgpu, chains, transitions):
     mo, so, emo, eso, eo = moments(zo)
     zm = np.abs(mg - mo) / np.sqrt(emg ** 2 + emo ** 2)
     zs = np.abs(sg - so) / np.sqrt(esg ** 2 + eso ** 2)
+    # what chance allows for n independent comparisons: n p3 + 3 sd + 1 beyond 3 MCSE, and all
+    # within the Bonferroni bound at a 1 % family-wise rate
+    from scipy.stats import norm
+
+    n = zm.size + zs.size
+    p3 = 2 * norm.sf(3.0)
     return {"oracle": "FP64 C restatement of numpyro's NUTS, %d chains x %d transitions from the GPU's "
                       "adapted state (%.0f s on %d host threads)" % (chains, transitions, res["sampling_s"],
                                                                     res["threads"]),
             "gpu_draws": "%d chains x %d draws" % zg.shape[:2],
             "max_abs_dmean_over_mcse": float(zm.max()), "max_abs_dsd_over_mcse": float(zs.max()),
             "coords_beyond_3_mcse": int(np.sum(zm > 3) + np.sum(zs > 3)), "coords": int(zg.shape[-1]),
+            "chance_allows_beyond_3": int(np.floor(n * p3 + 3 * np.sqrt(n * p3 * (1 - p3)) + 1)),
+            "bonferroni_bound": float(norm.isf(0.005 / n)),
             "oracle_min_bulk_ess": float(eo.min())}
 
 
@@ -679,10 +688,16 @@ def _tc_available():
         return False
 
 
+# special-function operations per logit of the tensor-core logistic epilogue (logreg_tc.cu,
+# epilogue_part): one ex2; tanh for half the rows; one rcp per 8 rows for the other half; one lg2
+# per 8 rows
+SFU_OPS_PER_LOGIT = 1.0 + 0.5 + 0.5 / 8 + 1.0 / 8
+
+
 def _sfu_roofline(launch_ms, n, chains):
-    """Special-function operations of one tensor-core potential launch (2.125 per logit: one
-    ex2, one tanh, one lg2 per 8 rows) per second, against the unit's peak measured on this GPU
-    for the same mix (gbn_measure_sfu)."""
+    """Special-function operations of one tensor-core potential launch (SFU_OPS_PER_LOGIT per
+    logit) per second, against the unit's peak measured on this GPU for the same mix
+    (gbn_measure_sfu)."""
     import torch
 
     from numpyro_gb300 import _lib
@@ -690,13 +705,13 @@ def _sfu_roofline(launch_ms, n, chains):
     peak = ctypes.c_double(0.0)
     rc = _lib.load().gbn_measure_sfu(ctypes.c_void_p(torch.cuda.current_stream().cuda_stream), 2,
                                      ctypes.byref(peak))
-    ops = 2.125 * n * chains
+    ops = SFU_OPS_PER_LOGIT * n * chains
     achieved = ops / (launch_ms * 1e-3)
     if rc != 0 or peak.value <= 0:
         return {"bound": "sfu", "achieved": achieved / 1e12, "peak": None, "unit": "Tops/s", "frac": None}
     return {"bound": "sfu", "achieved": achieved / 1e12, "peak": peak.value / 1e12, "unit": "Tops/s",
-            "frac": achieved / peak.value, "ops_per_launch": ops, "ops_per_logit": 2.125,
-            "peak_kind": "measured in this run (gbn_measure_sfu: the epilogue's ex2/tanh/lg2 mix on every SM)"}
+            "frac": achieved / peak.value, "ops_per_launch": ops, "ops_per_logit": SFU_OPS_PER_LOGIT,
+            "peak_kind": "measured in this run (gbn_measure_sfu: the epilogue's ex2/tanh/rcp/lg2 mix on every SM)"}
 
 
 def _launches_per_tick(precision):

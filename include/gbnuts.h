@@ -216,10 +216,18 @@ const char* gbn_tuning(gbn_handle h);
 int gbn_time_potential(gbn_handle h, void* stream, int32_t reps, float* ms);
 /* Measurement utility, no counterpart in the reference: the peak throughput (operations per
  * second, whole GPU) of the special-function unit on the operations of the tensor-core logistic
- * epilogue -- mode 0 ex2.approx, 1 tanh.approx, 2 their mix in the epilogue's proportion (8 ex2,
- * 8 tanh, 1 lg2) -- measured with independent dependency chains on every SM (a few ms).  The
+ * epilogue -- mode 0 ex2.approx, 1 tanh.approx, 2 the epilogue's mix (per 16 logits 16 ex2,
+ * 8 tanh, 1 rcp, 2 lg2) -- measured with independent dependency chains on every SM (a few ms).  The
  * roofline of that kernel's special-function work is taken against it. */
 int gbn_measure_sfu(void* stream, int32_t mode, double* ops_per_second);
+
+/* Diagnostic, no counterpart in the reference: for a tensor-core logistic handle, how many of the
+ * 128-chain blocks of its last potential launch took all three bf16 terms of the coefficients
+ * (the others took two and a first-order term, exact to 1e-3; logreg_tc.cu), of how many blocks,
+ * and the bound on a block's largest sum of squares of the third terms below which it takes two
+ * (negative: always three).  Other handles report 0 blocks.  Call between runs (it waits for the
+ * device). */
+int gbn_logreg_terms(gbn_handle h, int32_t* three_term_blocks, int32_t* blocks, float* two_term_limit);
 
 /* Largest num_points accepted by gbn_logreg_potential_noalloc. */
 #define GBN_NOALLOC_MAX_POINTS 256

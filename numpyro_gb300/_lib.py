@@ -137,6 +137,8 @@ EXPORTS = {
     "gbn_get_stats": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Stats)]),
     "gbn_tuning": (ctypes.c_char_p, [ctypes.c_void_p]),
     "gbn_measure_sfu": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.POINTER(ctypes.c_double)]),
+    "gbn_logreg_terms": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int32),
+                                        ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_float)]),
     "gbn_time_potential": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32,
                                           ctypes.POINTER(ctypes.c_float)]),
     "gbn_logreg_potential_noalloc": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,

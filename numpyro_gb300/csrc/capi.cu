@@ -71,6 +71,8 @@ static void refresh_fusion(gbn_handle h) {
   P.lrf_part_ll = nullptr;
   P.lrf_lin = nullptr;
   P.lrf_bsplit = nullptr;
+  P.lrf_split3 = nullptr;
+  P.lrf_e_tanh = 0;
   if (h->fuse_tick && !h->persistent && h->m.family == GBN_FAMILY_LOGREG && h->m.precision == GBN_PREC_BF16X3 &&
       h->m.tc && !logreg_tc_fusion(h->m, h->C, &P))
     P.lrf_part_g = nullptr;
@@ -874,6 +876,22 @@ int gbn_measure_sfu(void* stream, int32_t mode, double* ops_per_second) {
   if (!ops_per_second || mode < 0 || mode > 2) return fail(nullptr, GBN_ERR_INVALID_ARG, "gbn_measure_sfu: bad argument");
   cudaError_t e = measure_sfu_rate(mode, (cudaStream_t)stream, ops_per_second);
   if (e != cudaSuccess) return cuda_fail(nullptr, e, "gbn_measure_sfu");
+  return GBN_OK;
+}
+
+int gbn_logreg_terms(gbn_handle h, int32_t* three_term_blocks, int32_t* blocks, float* two_term_limit) {
+  if (!h || !three_term_blocks || !blocks || !two_term_limit)
+    return fail(h, GBN_ERR_INVALID_ARG, "gbn_logreg_terms: null argument");
+  *three_term_blocks = 0;
+  *blocks = 0;
+  *two_term_limit = -1.0f;
+  if (h->m.family != GBN_FAMILY_LOGREG || !h->m.tc) return GBN_OK;
+  cudaError_t e = cudaDeviceSynchronize();
+  int three = 0, nb = 0;
+  if (e == cudaSuccess) e = logreg_tc_terms(h->m, &three, &nb, two_term_limit);
+  if (e != cudaSuccess) return cuda_fail(h, e, "gbn_logreg_terms");
+  *three_term_blocks = three;
+  *blocks = nb;
   return GBN_OK;
 }
 

@@ -283,6 +283,8 @@ struct __align__(16) AdvParams {
   double lrf_pe_const;
   float lrf_inv_var;
   int32_t lrf_row_groups;
+  const int32_t* lrf_split3;  // per 128-chain block: 1 if the launch took three coefficient terms
+  int32_t lrf_e_tanh;         // GEMM2 summed tanh(l'/2) X' (see lr_finish.cuh)
 };
 
 // ---------------------------------------------------------------- groups

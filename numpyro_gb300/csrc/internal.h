@@ -130,6 +130,8 @@ bool logreg_tc_supported(const ModelDev& m);
 cudaError_t logreg_tc_prepare(ModelDev& m, int points);
 void logreg_tc_free(ModelDev& m);
 int logreg_tc_error(const ModelDev& m);  // nonzero: a device wait timed out
+// blocks of the last launch that took three coefficient terms, of how many; the two-term limit
+cudaError_t logreg_tc_terms(const ModelDev& m, int* three, int* blocks, float* limit);
 int* logreg_tc_error_ptr(const ModelDev& m);  // device address of that error word (or null)
 cudaError_t logreg_tc_launch(ModelDev& m, const float* Q, int npts, double* PE, float* G, const int32_t* pending,
                              cudaStream_t st, bool fused_tick = false);

@@ -8,29 +8,37 @@
 //
 // Sign-flipped rows.  With s_n = 1 - 2 y_n and X'_n = s_n X_n (exact in bf16):
 //   softplus(l_n) - y_n l_n = softplus(l'_n) = l'_n/2 + |l'_n|/2 + log(1 + e^{-|l'_n|}),  l' = X' b
-//   sum_n (sigmoid(l_n) - y_n) X_n = sum_n sigmoid(l'_n) X'_n
-// so the kernel never reads y: it streams X' and the linear part sum_n l'_n / 2 = (X'^T 1 / 2) . b
-// is added per chain from a vector computed once.
+//   sum_n (sigmoid(l_n) - y_n) X_n = sum_n sigmoid(l'_n) X'_n = (sum_n tanh(l'_n/2) X'_n + X'^T 1) / 2
+// so the kernel never reads y: it streams X', and the linear part sum_n l'_n / 2 = (X'^T 1 / 2) . b
+// is added per chain from a vector computed once (lr_finish.cuh).
 //
 // One CTA owns 128 chains and a strided set of 128-row tiles of X':
 //   warp 0      TMA producer: X' tile [128 rows x 64 feat] bf16, 128B swizzle, 8-stage ring,
 //               with an L2 prefetch running 8 tiles ahead
-//   warp 1      MMA issuer:  GEMM1  H[128 chains x 128 rows] = (b_hi + b_mid + b_lo)/2 . X'_tile^T
-//                            (three K=64 BF16 products accumulate in FP32 in TMEM, so the
-//                            FP32 coefficients are represented exactly: "bf16x3"),
-//                            GEMM2  G[128 chains x 64 feat] += E . X'_tile  (E = sigmoid(l'),
+//   warp 1      MMA issuer:  GEMM1  H[128 chains x 128 rows] = (b_hi + b_mid [+ b_lo])/2 . X'_tile^T
+//                            (K = 64 BF16 products accumulating in FP32 in TMEM: with all three
+//                            terms the FP32 coefficients are represented exactly; see below),
+//                            GEMM2  G[128 chains x 64 feat] += E . X'_tile  (E = tanh(l'/2),
 //                            the A operand read from TMEM)
 //   warps 2..17 epilogue: TMEM lanes are chains, columns rows.  Two groups of 8 warps take
 //               alternate tiles; in a group 2 warps per lane quadrant split the 128 rows.  Per
-//               logit one ex2 and one tanh; log(1 + e^{-|l'|}) is taken as one lg2 of the product
-//               of 8 rows' factors (2.125 special-function ops per logit).  E goes back to TMEM
-//               as bf16 pairs, into columns of the same H buffer the warp has already read.
+//               logit one ex2; E by tanh for half the rows and from the ex2 with one reciprocal
+//               per 8 rows for the other half; log(1 + e^{-|l'|}) as one lg2 of the product of 8
+//               rows' factors (1.6875 special-function ops per logit; epilogue_part).  E goes back
+//               to TMEM as bf16 pairs, into columns of the same H buffer the warp has already read.
 //               Each thread accumulates its chain's log-likelihood over its rows; the four
 //               threads of a chain are combined once per CTA in FP64.
 // Three H buffers in TMEM (3 x 128 columns) keep three tiles in flight, and GEMM2 of tile t is
 // issued after GEMM1 of tile t + 2; G lives in TMEM for the whole launch (64 columns).  Keeping
 // E in TMEM leaves shared memory to the X' and coefficient operands: with E in shared memory
 // as well (its stores plus GEMM2 reading it), the tensor pipe waited on shared-memory bandwidth.
+//
+// Two or three coefficient terms.  b/2 = hi + mid + lo exactly (bf16 each, |lo| <= 2^-17 |b/2|).
+// The third GEMM1 product (a third of GEMM1) is left out when the first-order term the finish adds
+// in its place, nu(b_hm) . b_lo (lr_finish.cuh), is exact to 1e-3: the remainder of that expansion
+// is at most (1/8) lambda_max(X^T X) |b_lo|^2 = (1/2) lambda_max |lo|^2, and the launch compares the
+// largest |lo|^2 over a block's 128 chains with 2e-3 / lambda_hat, lambda_hat a Gershgorin bound on
+// lambda_max(X^T X) formed once per model (far below the FP32 rounding of U's row sums).  The block's choice is recorded per launch (split3) for the finish.
 // The design matrix must be exactly representable in bf16 (checked on the host).
 // Every mbarrier wait is bounded; on a timeout the CTA records an error, drains its
 // in-flight copies and MMAs (bounded), frees TMEM and returns.
@@ -38,7 +46,10 @@
 #include <cudaTypedefs.h>
 #include <cuda_bf16.h>
 
+#include <algorithm>
+#include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <vector>
 
 #include "common.cuh"
@@ -77,19 +88,30 @@ enum { B_XFULL = 0, B_XEMPTY = STAGES, B_ACCF = 2 * STAGES, B_SF = B_ACCF + NBUF
 static_assert(LAG < NBUF, "GEMM1 of tile i reuses the buffer GEMM2 of tile i - NBUF reads");
 static_assert(ACC2_COL + BK <= TMEM_COLS, "TMEM holds the H buffers and G");
 static_assert(SMEM_BYTES <= 232448, "shared memory per CTA");
-static_assert(NUM_BARS * 8 + 8 <= 256, "barriers, TMEM address and abort flag fit their slot");
+static_assert(NUM_BARS * 8 + 8 + 16 <= 256, "barriers, TMEM address, abort flag and |lo|^2 maxima fit their slot");
 
 // One part of the epilogue for one warp: its lane's chain x 32 rows (TMEM columns at th).
 // TMEM holds h = l'/2 (the coefficients enter GEMM1 halved, an exact scaling).  Per row:
-//   E = sigmoid(l') = tanh(h)/2 + 1/2                      -> bf16, GEMM2's A operand in TMEM
-//       (forming it from e^{-2|h|} on the FMA pipe, with one reciprocal per 8 rows or by
-//       Newton's method, measured slower)
-//   softplus(l') - l'/2 = |h| + log(1 + e^{-2|h|})          -> |h| summed, the logs taken as
-//                                                            one log2 per product of 8 rows
+//   softplus(l') - l'/2 = |h| + log(1 + t),  t = e^{-2|h|} = e^{-|l'|}   (one ex2)
+//       |h| summed; the logs taken as one lg2 per product of 8 rows' (1 + t)
+//   E = tanh(h) = 2 sigmoid(l') - 1   -> bf16, GEMM2's A operand in TMEM
+//       (GEMM2 then gives sum_r tanh(h_r) X'_r = 2 (sum_r sigmoid(l'_r) X'_r) - X'^T 1: the
+//        finish halves it and adds X'^T 1 / 2, the vector the linear term already uses)
+// The 32 rows are 4 groups of 8.  tanh runs on the special-function unit at half the rate of
+// ex2, so the first RCP_GROUPS groups form E from the t already computed instead: with
+// u_j = 1 + t_j, one reciprocal R = 1 / (u_0 ... u_7) and prefix products P_j = u_0 ... u_j,
+// 1 / u_j = P_{j-1} (R u_7 ... u_{j+1}) and tanh(|h_j|) = 2 / u_j - 1 (relative error ~1e-6,
+// FP32 products).  The other groups use tanh.  With every group on one path or the other, one
+// unit or the other was the wall (measured at 1024 chains x 581,012 rows: all tanh 0.253 ms, all
+// reciprocal 0.282 ms; with the FP32 pair arithmetic below and two coefficient terms, one group
+// in four 0.219 ms, two 0.213 ms).  Pairs of rows share FP32x2 instructions (ex2 arguments, the
+// products) to save issue slots.
 // With MASK, rows r >= nvalid lie past the end of the data: they are left out of the
 // log-likelihood (their X' rows are zero, so E needs no mask).
 // E goes to the 16 TMEM columns at te, two rows per column (the even row in the low half):
 // columns this warp has already read, so H and E share the buffer.
+constexpr int RCP_GROUPS = 2;
+
 template <bool MASK>
 __device__ __forceinline__ void epilogue_part(uint32_t th, uint32_t te, int nvalid, float& sabs, float& slg) {
   const float NEG_2LOG2E = -2.8853900817779268f;
@@ -102,24 +124,67 @@ __device__ __forceinline__ void epilogue_part(uint32_t th, uint32_t te, int nval
   uint32_t pk[16];
 #pragma unroll
   for (int g8 = 0; g8 < 4; ++g8) {
-    float prod = 1.0f;
+    const bool full = !MASK || 8 * g8 + 8 <= nvalid;
+    if (g8 < RCP_GROUPS && full) {
+      float hv[8], tv[8], pp[8];
 #pragma unroll
-    for (int e = 0; e < 8; e += 2) {
-      float ev[2];
-#pragma unroll
-      for (int hh = 0; hh < 2; ++hh) {
-        const int r = 8 * g8 + e + hh;
-        const float h = __uint_as_float(v[r >> 4][r & 15]);
-        const float t = ex2_approx(fabsf(h) * NEG_2LOG2E);  // e^{-|l'|}
-        if (!MASK || r < nvalid) {
-          ta += fabsf(h);
-          prod = fmaf(prod, t, prod);  // prod * (1 + t), one rounding
-        }
-        ev[hh] = fmaf(0.5f, tanh_approx(h), 0.5f);
+      for (int j = 0; j < 8; j += 2) {
+        const int r = 8 * g8 + j;
+        hv[j] = __uint_as_float(v[r >> 4][r & 15]);
+        hv[j + 1] = __uint_as_float(v[(r + 1) >> 4][(r + 1) & 15]);
+        const float2 a = __fmul2_rn(make_float2(hv[j], hv[j + 1]), make_float2(NEG_2LOG2E, NEG_2LOG2E));
+        tv[j] = ex2_approx(-fabsf(a.x));
+        tv[j + 1] = ex2_approx(-fabsf(a.y));
+        ta += fabsf(hv[j]);
+        ta += fabsf(hv[j + 1]);
       }
-      pk[4 * g8 + (e >> 1)] = pack_bf16(ev[0], ev[1]);
+      pp[0] = 1.0f + tv[0];
+#pragma unroll
+      for (int j = 1; j < 8; ++j) pp[j] = fmaf(pp[j - 1], tv[j], pp[j - 1]);
+      float q = rcp_approx(pp[7]);  // q = 1 / P_j, from j = 7 down
+      float ev[8];
+#pragma unroll
+      for (int j = 7; j >= 0; --j) {
+        const float inv_u = j == 0 ? q : pp[j > 0 ? j - 1 : 0] * q;
+        ev[j] = copysignf(fmaf(2.0f, inv_u, -1.0f), hv[j]);
+        if (j > 0) q = fmaf(q, tv[j], q);
+      }
+#pragma unroll
+      for (int j = 0; j < 8; j += 2) pk[4 * g8 + (j >> 1)] = pack_bf16(ev[j], ev[j + 1]);
+      tl += lg2_approx(pp[7]);
+    } else if (full) {
+      float2 prod = make_float2(1.0f, 1.0f);
+#pragma unroll
+      for (int e = 0; e < 8; e += 2) {
+        const int r = 8 * g8 + e;
+        const float h0 = __uint_as_float(v[r >> 4][r & 15]), h1 = __uint_as_float(v[(r + 1) >> 4][(r + 1) & 15]);
+        const float2 a = __fmul2_rn(make_float2(h0, h1), make_float2(NEG_2LOG2E, NEG_2LOG2E));
+        const float t0 = ex2_approx(-fabsf(a.x)), t1 = ex2_approx(-fabsf(a.y));  // e^{-|l'|}
+        ta += fabsf(h0);
+        ta += fabsf(h1);
+        prod = __ffma2_rn(prod, make_float2(t0, t1), prod);  // prod * (1 + t), one rounding
+        pk[4 * g8 + (e >> 1)] = pack_bf16(tanh_approx(h0), tanh_approx(h1));
+      }
+      tl += lg2_approx(prod.x * prod.y);
+    } else {
+      float prod = 1.0f;
+#pragma unroll
+      for (int e = 0; e < 8; e += 2) {
+        float ev[2];
+#pragma unroll
+        for (int hh = 0; hh < 2; ++hh) {
+          const int r = 8 * g8 + e + hh;
+          const float h = __uint_as_float(v[r >> 4][r & 15]);
+          if (r < nvalid) {
+            ta += fabsf(h);
+            prod = fmaf(prod, ex2_approx(fabsf(h) * NEG_2LOG2E), prod);
+          }
+          ev[hh] = tanh_approx(h);
+        }
+        pk[4 * g8 + (e >> 1)] = pack_bf16(ev[0], ev[1]);
+      }
+      tl += lg2_approx(prod);
     }
-    tl += lg2_approx(prod);
   }
   tmem_st16(te, pk);
   sabs += ta;
@@ -135,6 +200,8 @@ struct Params {
   double* part_ll;  // [row_groups][npts]
   int* err;
   const int32_t* pending;
+  float lo2_limit;  // largest |lo|^2 of a block's chains for two coefficient terms (< 0: always three)
+  int32_t* split3;  // [chain blocks]: 1 where the launch took three terms (written by row group 0)
 };
 
 __global__ void __launch_bounds__(NUM_THREADS, 1) logreg_tc_kernel(const __grid_constant__ CUtensorMap tmap_x,
@@ -167,7 +234,26 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) logreg_tc_kernel(const __grid_
     *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
+  float* lo2_slot = reinterpret_cast<float*>(smem + OFF_MISC + NUM_BARS * 8 + 8);
   for (int i = threadIdx.x; i < BN; i += NUM_THREADS) ll_smem[i] = 0.0;
+  // |lo|^2 of each chain of the block (threads 0..127, four whole warps), maximum per warp
+  if (threadIdx.x < BN) {
+    const uint4* lo = reinterpret_cast<const uint4*>(P.bsplit + ((size_t)(cb * BN + threadIdx.x) * NSPLIT + 2) * BK);
+    float s2 = 0.0f;
+#pragma unroll
+    for (int k = 0; k < BK / 8; ++k) {
+      const uint4 u = lo[k];
+      const uint32_t w[4] = {u.x, u.y, u.z, u.w};
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const float a = __uint_as_float(w[j] << 16), b = __uint_as_float(w[j] & 0xffff0000u);
+        s2 = fmaf(a, a, fmaf(b, b, s2));
+      }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s2 = fmaxf(s2, __shfl_xor_sync(0xffffffffu, s2, o));
+    if (lane == 0) lo2_slot[warp] = s2;
+  }
   // coefficient splits -> K-major 128B-swizzled tiles [128 chains][64 feat] (one per split)
   {
     const uint4* src = reinterpret_cast<const uint4*>(P.bsplit + (size_t)cb * BN * NSPLIT * BK);
@@ -191,6 +277,9 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) logreg_tc_kernel(const __grid_
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = *tmem_holder;
+  const float lo2max = fmaxf(fmaxf(lo2_slot[0], lo2_slot[1]), fmaxf(lo2_slot[2], lo2_slot[3]));
+  const int nsplit = lo2max > P.lo2_limit ? 3 : 2;
+  if (threadIdx.x == 0 && rg == 0 && P.split3) P.split3[cb] = nsplit == 3 ? 1 : 0;
 
   if (warp == 0) {
     // ------------------------------------------------------------ TMA producer
@@ -248,6 +337,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) logreg_tc_kernel(const __grid_
         const uint64_t xs = sdesc_at(dx1, (uint32_t)(si * X_TILE));
 #pragma unroll
         for (int k = 0; k < NSPLIT; ++k) {
+          if (k >= nsplit) break;
 #pragma unroll
           for (int kk = 0; kk < BK / 16; ++kk)
             mma_bf16_warp(d, sdesc_at(dcoef, k * B_TILE + kk * 32), sdesc_at(xs, kk * 32), ID1,
@@ -403,10 +493,43 @@ __global__ void linear_term_kernel(const float* __restrict__ x, const float* __r
   if (rl == 0 && d < p) atomicAdd(&lin[d], part[0][d] + part[1][d] + part[2][d] + part[3][d]);
 }
 
+// X^T X (p <= 64) in FP64 from FP32 partials over 32-row chunks staged in shared memory, for the
+// Gershgorin bound on its largest eigenvalue.  256 threads, 16 entries of the 64 x 64 matrix each.
+__global__ void __launch_bounds__(256) gram_kernel(const float* __restrict__ x, int64_t n, int p,
+                                                   double* __restrict__ gram) {
+  __shared__ float xs[32][BK];
+  float acc[16];
+#pragma unroll
+  for (int k = 0; k < 16; ++k) acc[k] = 0.0f;
+  for (int64_t r0 = (int64_t)blockIdx.x * 32; r0 < n; r0 += (int64_t)gridDim.x * 32) {
+    __syncthreads();
+    for (int i = threadIdx.x; i < 32 * BK; i += blockDim.x) {
+      const int rr = i / BK, d = i % BK;
+      const int64_t r = r0 + rr;
+      xs[rr][d] = (r < n && d < p) ? x[r * p + d] : 0.0f;
+    }
+    __syncthreads();
+    for (int rr = 0; rr < 32; ++rr) {
+#pragma unroll
+      for (int k = 0; k < 16; ++k) {
+        const int e = threadIdx.x + k * 256;
+        acc[k] = fmaf(xs[rr][e / BK], xs[rr][e % BK], acc[k]);
+      }
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < 16; ++k) {
+    const int e = threadIdx.x + k * 256;
+    if (e / BK < p && e % BK < p) atomicAdd(&gram[e], (double)acc[k]);
+  }
+}
+
 struct TCState {
   double* lin = nullptr;
   __nv_bfloat16* xb = nullptr;
   __nv_bfloat16* bsplit = nullptr;
+  int32_t* split3 = nullptr;  // [bsplit_pts / 128]
+  float lo2_limit = -1.0f;    // < 0: always three coefficient terms
   CUtensorMap tmap;
   int* err = nullptr;
   int bsplit_pts = 0;
@@ -469,6 +592,28 @@ cudaError_t logreg_tc_prepare(ModelDev& m, int points) {
     if (r != CUDA_SUCCESS) return cudaErrorInvalidValue;
     e = cudaFuncSetAttribute(tc::logreg_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, tc::SMEM_BYTES);
     if (e != cudaSuccess) return e;
+    // two coefficient terms where |lo|^2 <= 2 tau / lambda_hat, tau = 1e-3 (see the file header);
+    // GBN_LOGREG_TERMS=3 keeps all three
+    const char* terms = getenv("GBN_LOGREG_TERMS");
+    if (!(terms && terms[0] == '3')) {
+      double* gram = nullptr;
+      e = cudaMalloc(&gram, sizeof(double) * tc::BK * tc::BK);
+      if (e != cudaSuccess) return e;
+      cudaMemset(gram, 0, sizeof(double) * tc::BK * tc::BK);
+      tc::gram_kernel<<<304, 256>>>(m.x, m.n, m.p, gram);
+      std::vector<double> g((size_t)tc::BK * tc::BK);
+      e = cudaMemcpy(g.data(), gram, sizeof(double) * g.size(), cudaMemcpyDeviceToHost);
+      cudaFree(gram);
+      if (e != cudaSuccess) return e;
+      double lam = 0.0;  // Gershgorin: lambda_max <= max_i sum_j |G_ij|
+      for (int i = 0; i < m.p; ++i) {
+        double row = 0.0;
+        for (int j = 0; j < m.p; ++j) row += std::fabs(g[(size_t)i * tc::BK + j]);
+        lam = std::max(lam, row);
+      }
+      lam *= 1.01;  // the FP32 partial sums' rounding
+      s->lo2_limit = lam > 0.0 ? (float)(2.0e-3 / lam) : 3.0e38f;
+    }
     s->ok = true;
   }
   int blocks = (points + tc::BN - 1) / tc::BN;
@@ -478,6 +623,11 @@ cudaError_t logreg_tc_prepare(ModelDev& m, int points) {
     e = cudaMalloc(&s->bsplit, sizeof(__nv_bfloat16) * (size_t)blocks * tc::BN * tc::NSPLIT * tc::BK);
     if (e != cudaSuccess) return e;
     cudaMemset(s->bsplit, 0, sizeof(__nv_bfloat16) * (size_t)blocks * tc::BN * tc::NSPLIT * tc::BK);
+    cudaFree(s->split3);
+    s->split3 = nullptr;
+    e = cudaMalloc(&s->split3, sizeof(int32_t) * (size_t)blocks);
+    if (e != cudaSuccess) return e;
+    cudaMemset(s->split3, 0, sizeof(int32_t) * (size_t)blocks);
     s->bsplit_pts = blocks * tc::BN;
   }
   return e;
@@ -489,6 +639,7 @@ void logreg_tc_free(ModelDev& m) {
   cudaFree(s->xb);
   cudaFree(s->lin);
   cudaFree(s->bsplit);
+  cudaFree(s->split3);
   cudaFree(s->err);
   delete s;
   m.tc = nullptr;
@@ -497,6 +648,20 @@ void logreg_tc_free(ModelDev& m) {
 int* logreg_tc_error_ptr(const ModelDev& m) {
   tc::TCState* s = reinterpret_cast<tc::TCState*>(m.tc);
   return s ? s->err : nullptr;
+}
+
+cudaError_t logreg_tc_terms(const ModelDev& m, int* three, int* blocks, float* limit) {
+  tc::TCState* s = reinterpret_cast<tc::TCState*>(m.tc);
+  *three = 0;
+  *blocks = 0;
+  *limit = s ? s->lo2_limit : -1.0f;
+  if (!s || !s->split3) return cudaSuccess;
+  std::vector<int32_t> v((size_t)s->bsplit_pts / tc::BN);
+  cudaError_t e = cudaMemcpy(v.data(), s->split3, sizeof(int32_t) * v.size(), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return e;
+  for (int32_t x : v) *three += x != 0;
+  *blocks = (int)v.size();
+  return cudaSuccess;
 }
 
 int logreg_tc_error(const ModelDev& m) {
@@ -509,7 +674,7 @@ int logreg_tc_error(const ModelDev& m) {
 
 void logreg_finish_launch(const float* Q, int npts, int ld, int p, int row_groups, const float* part_g,
                           const double* part_ll, const double* lin, double prior_scale, double* PE, float* G,
-                          const int32_t* pending, cudaStream_t st);
+                          const int32_t* pending, cudaStream_t st, const int32_t* split3, bool e_tanh);
 
 // row groups of a launch over npts points: the grid fills the SMs with (chain blocks x row groups)
 static int logreg_tc_row_groups(const ModelDev& m, int npts) {
@@ -531,6 +696,8 @@ bool logreg_tc_fusion(const ModelDev& m, int npts, AdvParams* P) {
   P->lrf_lin = s->lin;
   P->lrf_bsplit = reinterpret_cast<uint16_t*>(s->bsplit);
   P->lrf_row_groups = logreg_tc_row_groups(m, npts);
+  P->lrf_split3 = s->split3;
+  P->lrf_e_tanh = 1;
   logreg_prior_consts(m.hyper[0], m.p, &P->lrf_inv_var, &P->lrf_pe_const);
   return true;
 }
@@ -549,10 +716,11 @@ cudaError_t logreg_tc_launch(ModelDev& m, const float* Q, int npts, double* PE, 
   if (!fused_tick)
     tc::split_coefs_kernel<<<(npad * tc::BK + 255) / 256, 256, 0, st>>>(Q, npts, m.D, m.p, npad, s->bsplit,
                                                                          pending);
-  tc::Params P{m.n, s->bsplit, npts, rg, m.part_g, m.part_ll, s->err, pending};
+  tc::Params P{m.n, s->bsplit, npts, rg, m.part_g, m.part_ll, s->err, pending, s->lo2_limit, s->split3};
   tc::logreg_tc_kernel<<<dim3(blocks, rg), tc::NUM_THREADS, tc::SMEM_BYTES, st>>>(s->tmap, P);
   if (!fused_tick)
-    logreg_finish_launch(Q, npts, m.D, m.p, rg, m.part_g, m.part_ll, s->lin, m.hyper[0], PE, G, pending, st);
+    logreg_finish_launch(Q, npts, m.D, m.p, rg, m.part_g, m.part_ll, s->lin, m.hyper[0], PE, G, pending, st,
+                         s->split3, true);
   return cudaGetLastError();
 }
 

@@ -142,7 +142,9 @@ struct Chain {
   // store, so one memory round trip covers UB elements (stores to one chain buffer and loads
   // from another could otherwise not be reordered by the compiler).  Each thread only ever
   // touches its own elements d = tid + k * NT, in increasing d, so results do not depend on UB.
-  static constexpr int UB = 4;
+  // A warp per chain (the hierarchical family, J up to a few hundred) gains from 8 loads in
+  // flight; a CTA per chain (T = 4096: 16 elements per thread) loses occupancy with 8 and keeps 4.
+  static constexpr int UB = NT == 32 ? 8 : 4;
 
   // 0.5 * r . (M^-1 r)
   __device__ double kinetic(const float* r) {
@@ -214,7 +216,7 @@ struct Chain {
   template <typename F>
   __device__ void sym_matvec(const float* A, const float* x, F&& use) {
     for (int d0 = g.tid; d0 < D; d0 += UB * NT) {
-      float acc[UB] = {0.0f, 0.0f, 0.0f, 0.0f};
+      float acc[UB] = {};
       for (int j = 0; j < D; ++j) {
         const float xj = x[j];
         const float* Aj = A + (size_t)j * ld + d0;
@@ -985,7 +987,7 @@ __global__ void __launch_bounds__(256) advance_kernel(const AdvParams* __restric
     const int ph = P.e.ctl[c].phase;
     if (ph == PH_LEAF || ph == PH_HMC || ph == PH_HEUR)
       logreg_finish_warp(P.e.Q, c, P.C, P.D, P.D, P.lrf_row_groups, P.lrf_part_g, P.lrf_part_ll, P.lrf_lin,
-                         P.lrf_inv_var, P.lrf_pe_const, P.e.PE, P.e.G, tid);
+                         P.lrf_inv_var, P.lrf_pe_const, P.e.PE, P.e.G, tid, P.lrf_split3, P.lrf_e_tanh != 0);
     __syncwarp();  // G and PE written by other lanes
   }
   if (c < P.C) {

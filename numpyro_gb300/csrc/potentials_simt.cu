@@ -183,12 +183,13 @@ __global__ void __launch_bounds__(256) logreg_simt_kernel(const float* __restric
 __global__ void logreg_finish_kernel(const float* __restrict__ Q, int npts, int ld, int p, int row_groups,
                                      const float* __restrict__ part_g, const double* __restrict__ part_ll,
                                      const double* __restrict__ lin, float inv_var_f, double pe_const,
-                                     double* __restrict__ PE, float* __restrict__ G, const int32_t* pending) {
+                                     double* __restrict__ PE, float* __restrict__ G, const int32_t* pending,
+                                     const int32_t* __restrict__ split3 = nullptr, bool e_tanh = false) {
   if (pending && *pending == 0) return;
   const int c = blockIdx.x * 8 + (threadIdx.x >> 5);
   if (c >= npts) return;
   logreg_finish_warp(Q, c, npts, ld, p, row_groups, part_g, part_ll, lin, inv_var_f, pe_const, PE, G,
-                     threadIdx.x & 31);
+                     threadIdx.x & 31, split3, e_tanh);
 }
 
 // 1 / s^2 (FP32, as the gradient uses it) and p (log(2 pi) / 2 + log s) of the Normal(0, s) prior
@@ -680,28 +681,31 @@ cudaError_t autotune_potential(ModelDev& m, const float* Q, int npts, double* PE
 
 // ============================================================ special-function throughput
 // Peak rate of the special-function unit for the operations of the tensor-core logistic epilogue
-// (ex2.approx, tanh.approx, lg2.approx), measured with independent dependency chains (8 per
-// thread) so the unit, not latency, sets the rate.  MIX issues them in the epilogue's proportion:
-// per 16 operations 8 ex2 + 8 tanh, plus one lg2 (the epilogue's 2.125 per logit).
+// (ex2.approx, tanh.approx, rcp.approx, lg2.approx), measured with independent dependency chains
+// (8 per thread) so the unit, not latency, sets the rate.  MIX issues them in the epilogue's
+// proportion: per 16 logits 16 ex2, 8 tanh, 1 rcp and 2 lg2 (1.6875 per logit).
 template <int MODE>
 __global__ void __launch_bounds__(256) sfu_rate_kernel(int iters, float* __restrict__ out) {
   float v[8];
 #pragma unroll
   for (int k = 0; k < 8; ++k) v[k] = 0.25f + 0.01f * (float)(k + (threadIdx.x & 7));
   for (int i = 0; i < iters; ++i) {
+    if (MODE == 2) {
 #pragma unroll
-    for (int k = 0; k < 8; ++k) {
-      float y;
-      if (MODE == 0 || (MODE == 2 && (k & 1) == 0))
-        asm volatile("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(-v[k]));
-      else
-        asm volatile("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(v[k]));
-      v[k] = y;
-    }
-    if (MODE == 2 && (i & 1)) {
-      float y;
-      asm volatile("lg2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(1.0f + v[0]));
-      v[0] = 0.5f * y;
+      for (int k = 0; k < 16; ++k) asm volatile("ex2.approx.ftz.f32 %0, %1;" : "=f"(v[k & 7]) : "f"(-v[k & 7]));
+#pragma unroll
+      for (int k = 0; k < 8; ++k) asm volatile("tanh.approx.f32 %0, %1;" : "=f"(v[k]) : "f"(v[k]));
+      asm volatile("rcp.approx.ftz.f32 %0, %1;" : "=f"(v[0]) : "f"(1.0f + v[0]));
+      asm volatile("lg2.approx.ftz.f32 %0, %1;" : "=f"(v[1]) : "f"(1.5f + v[1]));
+      asm volatile("lg2.approx.ftz.f32 %0, %1;" : "=f"(v[2]) : "f"(1.5f + v[2]));
+    } else {
+#pragma unroll
+      for (int k = 0; k < 8; ++k) {
+        if (MODE == 0)
+          asm volatile("ex2.approx.ftz.f32 %0, %1;" : "=f"(v[k]) : "f"(-v[k]));
+        else
+          asm volatile("tanh.approx.f32 %0, %1;" : "=f"(v[k]) : "f"(v[k]));
+      }
     }
   }
   float acc = 0.0f;
@@ -737,8 +741,8 @@ cudaError_t measure_sfu_rate(int mode, cudaStream_t st, double* ops_per_s) {
   if (e == cudaSuccess) e = cudaEventSynchronize(b);
   float ms = 0.0f;
   if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, a, b);
-  // operations per launch: 8 chains x iters per thread, plus the mix's lg2 every other iteration
-  const double per_thread = 8.0 * iters + (mode == 2 ? iters / 2 : 0);
+  // operations per launch: per thread and iteration 8 (one per chain), or the mix's 27
+  const double per_thread = (mode == 2 ? 27.0 : 8.0) * iters;
   if (e == cudaSuccess) *ops_per_s = per_thread * blocks * threads * reps / (ms * 1e-3);
   if (a) cudaEventDestroy(a);
   if (b) cudaEventDestroy(b);
@@ -788,11 +792,11 @@ void horseshoe_finish_launch(const float* Q, int npts, int ld, int P, int64_t N,
 
 void logreg_finish_launch(const float* Q, int npts, int ld, int p, int row_groups, const float* part_g,
                           const double* part_ll, const double* lin, double prior_scale, double* PE, float* G,
-                          const int32_t* pending, cudaStream_t st) {
+                          const int32_t* pending, cudaStream_t st, const int32_t* split3, bool e_tanh) {
   float ivf;
   double pec;
   logreg_prior_consts(prior_scale, p, &ivf, &pec);
   logreg_finish_kernel<<<(npts + 7) / 8, 256, 0, st>>>(Q, npts, ld, p, row_groups, part_g, part_ll, lin, ivf, pec, PE,
-                                                       G, pending);
+                                                       G, pending, split3, e_tanh);
 }
 }  // namespace gbn

@@ -130,6 +130,104 @@ def test_logreg_tc_matches_fp32_path_full_size():
     k32.close()
 
 
+def _terms(kernel):
+    import ctypes
+
+    from numpyro_gb300 import _lib
+
+    three, blocks, limit = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_float()
+    _lib.check(_lib.load().gbn_logreg_terms(kernel._handle, ctypes.byref(three), ctypes.byref(blocks),
+                                            ctypes.byref(limit)), kernel._handle)
+    return three.value, blocks.value, limit.value
+
+
+def _lo2(z):
+    """Sum over coefficients of the squared third bf16 term of z / 2 (the split's arithmetic)."""
+    from numpyro_gb300.datasets import _round_bf16
+
+    h = (0.5 * np.asarray(z, np.float32)).astype(np.float32)
+    r1 = (h - _round_bf16(h)).astype(np.float32)
+    r2 = (r1 - _round_bf16(r1)).astype(np.float32)
+    return np.sum(r2.astype(np.float64) ** 2, axis=-1)
+
+
+@pytest.mark.gpu
+def test_logreg_tc_two_coefficient_terms_agree_with_three(monkeypatch):
+    """The tensor-core kernel leaves out the third bf16 term of the coefficients when the
+    first-order energy term added in its place is exact to 1e-3 (covtype-like data: the
+    remainder bound is ~1e-7); its energies must then match the kernel run with all three
+    terms (GBN_LOGREG_TERMS=3) and the FP64 oracle, and its limit must be 2e-3 over the
+    Gershgorin bound on lambda_max(X^T X)."""
+    _tc_or_skip()
+    from numpyro_gb300 import datasets, models
+
+    X, y, beta = datasets.covtype_like(seed=2, n=40_000)
+    rng = np.random.default_rng(3)
+    z = (beta[None, :] + 0.02 * rng.standard_normal((256, X.shape[1]))).astype(np.float32)
+    zt = torch.as_tensor(z, device="cuda")
+    k2 = NUTS(models.LogisticRegression(X, y), num_chains=256, precision="bf16x3")
+    pe2, g2 = [t.cpu().numpy() for t in k2.potential_and_grad(zt)]
+    three, blocks, limit = _terms(k2)
+    k2.close()
+    gram = X.T.astype(np.float64) @ X.astype(np.float64)
+    lam = np.max(np.sum(np.abs(gram), axis=1))
+    np.testing.assert_allclose(limit, 2e-3 / (1.01 * lam), rtol=1e-4)
+    assert (three, blocks) == (0, 2), (three, blocks, limit, _lo2(z).max())
+    monkeypatch.setenv("GBN_LOGREG_TERMS", "3")
+    k3 = NUTS(models.LogisticRegression(X, y), num_chains=256, precision="bf16x3")
+    pe3, g3 = [t.cpu().numpy() for t in k3.potential_and_grad(zt)]
+    assert _terms(k3)[:2] == (2, 2)
+    k3.close()
+    print("two vs three terms: max |dU| %.3e (U ~ %.3e)" % (np.max(np.abs(pe2 - pe3)), np.abs(pe3).max()))
+    assert np.max(np.abs(pe2 - pe3)) <= 2e-7 * np.abs(pe3).max() + 1e-3
+    scale = np.max(np.abs(g3), axis=1, keepdims=True)
+    assert np.max(np.abs(g2 - g3) / scale) < 3e-3
+    X64, y64 = X.astype(np.float64), y.astype(np.float64)
+    for c in (0, 101, 255):
+        pr = PR.logreg_potential(z[c].astype(np.float64), X64, y64)
+        assert abs(pe2[c] - pr) <= 1e-6 * abs(pr) + 1e-3, (c, pe2[c], pr)
+
+
+@pytest.mark.gpu
+def test_logreg_tc_takes_three_terms_where_a_block_needs_them(monkeypatch):
+    """Coefficients of +-1000 on two identical columns in the chains of one 128-chain block only:
+    their third bf16 terms (~4e-3) put that block over the limit, so it (and only it) takes all
+    three terms, and gives what a run that always takes three gives (the gradient bit for bit; the
+    energy to FP64 rounding, as a chain's four per-thread sums meet in FP64 shared-memory atomics)."""
+    _tc_or_skip()
+    from numpyro_gb300 import datasets, models
+
+    rng = np.random.default_rng(11)
+    n, p, C = 5000, 6, 256
+    X = np.empty((n, p), np.float32)
+    x = datasets._round_bf16(rng.standard_normal(n).astype(np.float32))
+    X[:, 0] = x
+    X[:, 1] = x
+    X[:, 2:-1] = datasets._round_bf16(rng.standard_normal((n, p - 3)).astype(np.float32))
+    X[:, -1] = 1.0
+    y = (rng.random(n) < 0.5).astype(np.float32)
+    z = (0.3 * rng.standard_normal((C, p))).astype(np.float32)
+    big = (1000.0 + 3.0 * rng.random(128)).astype(np.float32)
+    z[128:, 0] += big
+    z[128:, 1] -= big
+    zt = torch.as_tensor(z, device="cuda")
+    model = models.LogisticRegression(X, y, prior_scale=2000.0)
+    k = NUTS(model, num_chains=C, precision="bf16x3")
+    pe, g = [t.cpu().numpy() for t in k.potential_and_grad(zt)]
+    three, blocks, limit = _terms(k)
+    k.close()
+    lo2 = _lo2(z)
+    print("limit %.3e; largest |lo|^2 block 0 %.3e, block 1 %.3e" % (limit, lo2[:128].max(), lo2[128:].max()))
+    assert lo2[:128].max() <= limit < lo2[128:].max()
+    assert (three, blocks) == (1, 2)
+    monkeypatch.setenv("GBN_LOGREG_TERMS", "3")
+    k3 = NUTS(model, num_chains=C, precision="bf16x3")
+    pe3, g3 = [t.cpu().numpy() for t in k3.potential_and_grad(zt)]
+    k3.close()
+    np.testing.assert_allclose(pe[128:], pe3[128:], rtol=1e-13)
+    np.testing.assert_array_equal(g[128:], g3[128:])
+
+
 TUNED = [c for c in CASES if c[0] in ("hier_nc", "logreg", "horseshoe", "horseshoe_nc")]
 
 
