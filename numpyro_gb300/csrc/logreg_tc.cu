@@ -75,7 +75,13 @@ constexpr int OFF_MISC = OFF_B + NSPLIT * B_TILE;
 constexpr int NUM_BARS = 2 * STAGES + 3 * NBUF + 1;
 constexpr int SMEM_BYTES = OFF_MISC + 256 + BN * 8 + 1024;  // + alignment slack
 constexpr int EPI_WARPS = 16;             // epilogue warps: 4 per TMEM lane quadrant
-constexpr int EPI_GROUP = EPI_WARPS / 2;  // warps that share one tile (groups take alternate tiles)
+// EPI_ALTERNATE: two groups of 8 warps take alternate tiles (each warp 64 rows of every other
+// tile); otherwise all 16 warps take every tile (each warp 32 rows of it).  Measured at 1024 chains
+// x 581,012 rows: alternate 0.211 ms, every tile 0.226 ms (the groups' TMEM loads and
+// special-function bursts interleave instead of coinciding).
+constexpr bool EPI_ALTERNATE = true;
+constexpr int EPI_GROUP = EPI_ALTERNATE ? EPI_WARPS / 2 : EPI_WARPS;  // warps that share one tile
+constexpr int EPI_ROWS = BM * 4 / EPI_GROUP;                         // rows of a tile per warp
 constexpr int GCOLS = BK * 4 / EPI_WARPS; // gradient columns read back per epilogue warp
 constexpr int NUM_THREADS = 32 * (2 + EPI_WARPS);
 constexpr uint32_t TMEM_COLS = 512;
@@ -356,9 +362,11 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) logreg_tc_kernel(const __grid_
         const uint64_t xs = sdesc_at(dx2, (uint32_t)(sj * X_TILE));
 #pragma unroll
         for (int kk = 0; kk < BM / 16; ++kk) {
-          // A = E rows 16kk..16kk+15: 8 TMEM columns in row half kk / 4 (rows 64 h + r at column
-          // 64 h + r / 2); B = X' tile, MN-major (features contiguous), 8-row groups 1024 B apart
-          mma_bf16_tmem_a_warp(tmem + ACC2_COL, ea + (uint32_t)((kk >> 2) * 64 + (kk & 3) * 8),
+          // A = E rows 16kk..16kk+15: 8 TMEM columns in the block of the warp that wrote them
+          // (rows EPI_ROWS w + r at column EPI_ROWS w + r / 2); B = X' tile, MN-major (features
+          // contiguous), 8-row groups 1024 B apart
+          constexpr int KW = EPI_ROWS / 16;  // K steps per epilogue warp's block of rows
+          mma_bf16_tmem_a_warp(tmem + ACC2_COL, ea + (uint32_t)((kk / KW) * EPI_ROWS + (kk % KW) * 8),
                                sdesc_at(xs, kk * 2048), ID2, (j > 0 || kk > 0) ? 1u : 0u);
         }
         mma_commit_warp(bar(B_SE + bj));
@@ -374,30 +382,29 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) logreg_tc_kernel(const __grid_
     }
   } else {
     // ------------------------------------------------------------ epilogue (warps 2..17)
-    // Two groups of 8 warps take alternate tiles, so that the groups' TMEM loads and
-    // special-function bursts interleave instead of coinciding.
-    // In a group, 2 warps per TMEM lane quadrant each take a 64-row half of the tile, as two
-    // 32-row parts.
+    // The EPI_GROUP warps that take a tile split its rows: EPI_ROWS per warp, the warps of each
+    // TMEM lane quadrant side by side, as 32-row parts.
     const int ew = warp - 2;
-    const int q = warp & 3;          // TMEM lane quadrant this warp may access: chains 32q..32q+31
-    const int grp = ew / EPI_GROUP;  // tiles i with i % 2 == grp
-    const int rh = (ew >> 2) & 1;    // row half of each tile: rows 64 rh .. 64 rh + 63
-    const int c = q * 32 + lane;     // this thread's chain within the CTA
-    const uint32_t tl = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(rh * 64);
+    const int q = warp & 3;                                  // TMEM lane quadrant: chains 32q..32q+31
+    const int grp = EPI_ALTERNATE ? ew / EPI_GROUP : 0;      // tiles i with i % NGRP == grp
+    constexpr int NGRP = EPI_WARPS / EPI_GROUP;
+    const int wr = (ew >> 2) % (EPI_GROUP / 4);              // this warp's block of rows in a tile
+    const int c = q * 32 + lane;                             // this thread's chain within the CTA
+    const uint32_t tl = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(wr * EPI_ROWS);
     Comp32 ll{0.0f, 0.0f};  // log-likelihood of this chain over this thread's rows, all tiles
     bool ok = true;
-    for (int i = grp; i < my_tiles && ok; i += 2) {
-      const int64_t row0 = ((int64_t)rg + (int64_t)i * P.row_groups) * BM + rh * 64;
+    for (int i = grp; i < my_tiles && ok; i += NGRP) {
+      const int64_t row0 = ((int64_t)rg + (int64_t)i * P.row_groups) * BM + wr * EPI_ROWS;
       const int b = i % NBUF;
       ok = bar_wait(bar(B_ACCF + b), (i / NBUF) & 1, abort_flag, P.err);
       if (!ok) break;
       tc_fence_after();
 #pragma unroll
-      for (int part = 0; part < 2; ++part) {
+      for (int part = 0; part < EPI_ROWS / 32; ++part) {
         float sabs = 0.0f, slg = 0.0f;
         const int64_t nleft = P.n - (row0 + part * 32);
-        // H of rows 64 rh + 32 part .. +31 is read from columns 64 rh + 32 part; their E goes to
-        // columns 64 rh + 16 part .. +15, which part 0 has already read
+        // H of the block's rows 32 part .. +31 is read from its columns 32 part ..; their E goes
+        // to its columns 16 part .. +15, which this warp has already read
         const uint32_t th = tl + (uint32_t)(b * BM + part * 32), te = tl + (uint32_t)(b * BM + part * 16);
         if (nleft >= 32)
           epilogue_part<false>(th, te, 32, sabs, slg);

@@ -70,7 +70,8 @@ def _gate(name, zg, zo, rhat_max=1.01, max_unconverged=0.0):
     assert np.mean(~conv) <= max_unconverged, (name, int(np.sum(~conv)))
     assert rg.max() < rhat_max, (name, rg.max())
     assert np.sum(z > 3.0) <= beyond3, (name, int(np.sum(z > 3.0)))
-    assert z.max() <= bound, (name, int(np.argmax(z)), z.max())
+    coord = np.flatnonzero(conv)[int(np.argmax(z)) % zm.size]
+    assert z.max() <= bound, (name, "mean" if np.argmax(z) < zm.size else "sd", int(coord), z.max())
 
 
 def _gpu_run(model, C, W, S, with_divergences=False, **kw):
