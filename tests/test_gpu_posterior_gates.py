@@ -51,19 +51,19 @@ def moment_bounds(n):
     return int(np.floor(n * p3 + 3 * np.sqrt(n * p3 * (1 - p3)) + 1)), float(norm.isf(0.005 / n))
 
 
-def _gate(name, zg, zo, rhat_max=1.01, max_unconverged=0.0):
+def _gate(name, zg, zo, rhat_max=1.01, max_unconverged=0.0, conv_rhat=1.01):
     """R-hat of the GPU chains below rhat_max; the moments of every coordinate that both samples
-    have converged on (split R-hat < 1.01: a Monte Carlo standard error means nothing otherwise)
+    have mixed on (split R-hat < conv_rhat: a Monte Carlo standard error means nothing otherwise)
     within what chance allows; at most max_unconverged of the coordinates left out."""
     mg, sg, emg, esg, eg, rg = _stats(zg)
     mo, so, emo, eso, eo, ro = _stats(zo)
-    conv = (rg < 1.01) & (ro < 1.01)
+    conv = (rg < conv_rhat) & (ro < conv_rhat)
     zm = (np.abs(mg - mo) / np.sqrt(emg ** 2 + emo ** 2))[conv]
     zs = (np.abs(sg - so) / np.sqrt(esg ** 2 + eso ** 2))[conv]
     z = np.concatenate([zm, zs])
     beyond3, bound = moment_bounds(z.size)
     print("%s: GPU R-hat max %.4f (oracle %.4f), min bulk-ESS GPU %.0f oracle %.0f; "
-          "max |dmean|/MCSE %.2f, max |dsd|/MCSE %.2f over %d converged coordinates (of %d); %d of %d comparisons "
+          "max |dmean|/MCSE %.2f, max |dsd|/MCSE %.2f over %d mixed coordinates (of %d); %d of %d comparisons "
           "beyond 3 MCSE (chance allows %d), all within %.2f"
           % (name, rg.max(), ro.max(), eg.min(), eo.min(), zm.max(), zs.max(), zm.size, conv.size, np.sum(z > 3),
              z.size, beyond3, bound))
@@ -115,20 +115,27 @@ def test_stochastic_volatility_posterior_gate():
 # coefficients leave funnels that some chains cross rarely).  So the GPU's R-hat is held to the
 # reference sampler's own range on the same posterior, chains and draws, and its divergence rate to
 # within half and one and a half times the oracle's.  The moments are compared on the coordinates
-# both samples have converged on; 27 to 35 of the 102 were left out in runs on GB300, and at most
-# half may be.
+# whose split R-hat is below 1.05 in both samples (at most a quarter may be left out), against 64
+# oracle chains: with 16, one coordinate's sd (0.846 +- 0.005) sat 5 of its Monte Carlo standard
+# errors below what 64 oracle chains (0.871) and four GPU runs (0.862-0.875) gave -- too few chains
+# for these heavy tails to estimate their own error.
 HORSESHOE_RHAT_OF_REFERENCE = 1.12
+
+
+@pytest.fixture(scope="module")
+def horseshoe_oracle():
+    X, y, _ = datasets.horseshoe_data(seed=3, n=200, p=50, nonzero=5)
+    model = models.HorseshoeRegression(X, y, noncentered=True)
+    return model, B.run_model(B.load("f64"), cmodel_of(model), model.latent_dim, 64, 1000, 3000, seed=SEED + 3)
 
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("precision", ["fp32", "bf16x3"])
-def test_horseshoe_posterior_gate(precision):
-    X, y, _ = datasets.horseshoe_data(seed=3, n=200, p=50, nonzero=5)
-    model = models.HorseshoeRegression(X, y, noncentered=True)
+def test_horseshoe_posterior_gate(precision, horseshoe_oracle):
+    model, res = horseshoe_oracle
     zg, _, dg = _gpu_run(model, 128, 1000, 3000, with_divergences=True, precision=precision)
-    res = B.run_model(B.load("f64"), cmodel_of(model), model.latent_dim, 16, 1000, 3000, seed=SEED + 3)
     _gate("horseshoe_nc N=200 P=50 %s" % precision, zg, res["samples"], rhat_max=HORSESHOE_RHAT_OF_REFERENCE,
-          max_unconverged=0.5)
+          max_unconverged=0.25, conv_rhat=1.05)
     fg, fo = dg.mean(), res["diverging"].mean()
     print("divergent transitions: GPU %.4f, oracle %.4f" % (fg, fo))
     assert 0.5 * fo <= fg <= 1.5 * fo, (fg, fo)
