@@ -128,8 +128,45 @@ __device__ __forceinline__ void epilogue_part(uint32_t th, uint32_t te, int nval
   tmem_wait16(v[1]);
   float ta = 0.0f, tl = 0.0f;
   uint32_t pk[16];
+  int g_first = 0;  // the first group the loop below takes
+  if (RCP_GROUPS == 2 && (!MASK || nvalid >= 16)) {
+    // groups 0 and 1 in the reciprocal form side by side, in the two halves of FP32x2 instructions
+    const float2 C2 = make_float2(NEG_2LOG2E, NEG_2LOG2E);
+    float ha[8], hb[8];
+    float2 tv[8], pp[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      ha[j] = __uint_as_float(v[0][j]);
+      hb[j] = __uint_as_float(v[0][8 + j]);
+      const float2 a = __fmul2_rn(make_float2(ha[j], hb[j]), C2);
+      tv[j] = make_float2(ex2_approx(-fabsf(a.x)), ex2_approx(-fabsf(a.y)));
+      ta += fabsf(ha[j]);
+      ta += fabsf(hb[j]);
+    }
+    pp[0] = __fadd2_rn(make_float2(1.0f, 1.0f), tv[0]);
+#pragma unroll
+    for (int j = 1; j < 8; ++j) pp[j] = __ffma2_rn(pp[j - 1], tv[j], pp[j - 1]);
+    float2 q = make_float2(rcp_approx(pp[7].x), rcp_approx(pp[7].y));  // 1 / P_j, from j = 7 down
+    float ea[8], eb[8];
+#pragma unroll
+    for (int j = 7; j >= 0; --j) {
+      const float2 inv_u = j == 0 ? q : __fmul2_rn(pp[j > 0 ? j - 1 : 0], q);
+      const float2 e = __ffma2_rn(inv_u, make_float2(2.0f, 2.0f), make_float2(-1.0f, -1.0f));
+      ea[j] = copysignf(e.x, ha[j]);
+      eb[j] = copysignf(e.y, hb[j]);
+      if (j > 0) q = __ffma2_rn(q, tv[j], q);
+    }
+#pragma unroll
+    for (int j = 0; j < 8; j += 2) {
+      pk[j >> 1] = pack_bf16(ea[j], ea[j + 1]);
+      pk[4 + (j >> 1)] = pack_bf16(eb[j], eb[j + 1]);
+    }
+    tl += lg2_approx(pp[7].x * pp[7].y);
+    g_first = 2;
+  }
 #pragma unroll
   for (int g8 = 0; g8 < 4; ++g8) {
+    if (g8 < g_first) continue;
     const bool full = !MASK || 8 * g8 + 8 <= nvalid;
     if (g8 < RCP_GROUPS && full) {
       float hv[8], tv[8], pp[8];
