@@ -26,15 +26,15 @@ float32 restatement does, less 1 % of the transitions, and on >= 97 % in any cas
 median position error and 99th-percentile accept-probability error may be at most 3 times
 the float32 restatement's (and are held to the FP32 bars above when those are larger).
 
-bf16x3 logistic: the gradient's residual E = sigmoid(X'b) enters the tensor cores rounded
-to bfloat16 (relative error <= 2^-9 per row); the energies (and so the acceptance and the
-multinomial choice) stay exact to FP32.  The leapfrog with any deterministic gradient field
-is still volume-preserving and reversible, so the target is unchanged; only the trajectory
-moves.  Summed over the rows the rounding leaves the gradient ~2e-3 of its scale off, and
-after a NUTS trajectory positions differ from FP64 by a few 1e-3 relative.  Measured on
-GB300: tree sizes identical on 1,024 of 1,024 transitions, median position error 3.7e-3,
-accept probabilities within 2e-2.  Bar: tree sizes >= 99 %, median position error < 1e-2,
-accept probabilities within 5e-2.
+bf16x3 logistic: the gradient's E = tanh(X'b/2) enters the tensor cores rounded to bfloat16
+(absolute error <= 2^-9 per row), and where the kernel takes the coefficients as two bf16 terms
+with a first-order energy term, the gradient is the one at that two-term value (2^-16 relative);
+the energies (and so the acceptance and the multinomial choice) stay exact to FP32.  The leapfrog
+with any deterministic gradient field is still volume-preserving and reversible, so the target is
+unchanged; only the trajectory moves.  Measured on GB300: tree sizes identical on 1,024 of 1,024
+transitions, median position error 6.3e-4, accept probabilities within 6e-3 (3.7e-3 and 2e-2 when E
+was sigmoid(X'b) in bfloat16).  Bar: tree sizes >= 99 %, median position error < 1e-2, accept
+probabilities within 5e-2.
 """
 import numpy as np
 import pytest
