@@ -115,40 +115,58 @@ def workload_run(w, precision=None, num_warmup=None, num_samples=None, diagnose=
     ticks = k.stats()["ticks"] - t_ticks
     ns = out["num_steps"].cpu().numpy()
     divergences = int(out["diverging"].sum().item())
+    # bulk-ESS and split R-hat of every coordinate, computed where the draws are (device_diagnostics);
+    # only the subsample the --diagnose comparison with the oracle needs comes to the host
+    from numpyro_gb300 import device_diagnostics as DD
+
+    zd = out["z"]
+    z = None
+    extra = {}
     if w in ("sv", "sv_nc"):
-        # every 16th step of the walk plus nu and s keeps the host-side ranking to ~260 coordinates;
-        # the non-centred run adds the derived walk h = s * cumsum(h_base) at the same steps
-        zd = out["z"]
         T = zd.shape[-1] - 2
-        idx = torch.tensor(list(range(0, T, 16)) + [T, T + 1], device=zd.device)
-        parts = [zd.index_select(2, idx)]
-        if w == "sv_nc":
-            h = torch.exp(zd[..., T + 1:].double()) * torch.cumsum(zd[..., :T].double(), dim=-1)
-            parts.append(h.index_select(2, idx[:-2]).float())
+        zall = zd
+        if w == "sv_nc":  # the derived walk h = s * cumsum(h_base) as well
+            h = (torch.exp(zd[..., T + 1:].double()) * torch.cumsum(zd[..., :T].double(), dim=-1)).float()
+            zall = torch.cat([zd, h], dim=2)
             del h
-        z = torch.cat(parts, dim=2).cpu().numpy()
-        del zd, parts
+        ess = DD.bulk_effective_sample_size(zall, chunk=256)
+        rhat = DD.split_gelman_rubin(zall, chunk=256)
+        ess_min, rhat_max = float(torch.nan_to_num(ess, nan=float("inf")).min()), float(torch.nan_to_num(rhat).max())
+        ess_note = "min over all %d latent coordinates%s, computed on the device" % (
+            zall.shape[-1], " and the derived walk h" if w == "sv_nc" else "")
+        del zall
+        if diagnose:
+            idx = torch.tensor(list(range(0, T, 16)) + [T, T + 1], device=zd.device)
+            z = zd.index_select(2, idx).cpu().numpy()
     elif w == "uneven_hier":
-        picked = list(range(0, model.num_models, 64))  # a strided sample of 64 models
-        rows = torch.tensor([4 * m + i for m in picked for i in range(4)], device=out["z"].device)
-        z = out["z"].index_select(0, rows).cpu().numpy()
+        M, cpm = model.num_models, C // model.num_models
+        Dmax = zd.shape[-1]
+        zm = zd.view(M, cpm, zd.shape[1], Dmax).permute(1, 2, 0, 3)  # [chains of a model, draws, model, coord]
+        ess = DD.bulk_effective_sample_size(zm, chunk=4096)
+        rhat = DD.split_gelman_rubin(zm, chunk=4096)
+        dims = torch.tensor([model.chain_latent_dim(cpm * m, cpm) for m in range(M)], device=zd.device)
+        valid = torch.arange(Dmax, device=zd.device)[None, :] < dims[:, None]  # padding excluded
+        ess_m = torch.where(valid, torch.nan_to_num(ess, nan=float("inf")), torch.full_like(ess, float("inf"))).min(dim=1).values
+        rhat_m = torch.where(valid, torch.nan_to_num(rhat), torch.zeros_like(rhat)).max(dim=1).values
+        ess_min, rhat_max = float(ess_m.min()), float(rhat_m.max())
+        ess_note = "min over all %d models of the per-model min bulk-ESS (its %d chains), computed on the device" % (
+            M, cpm)
+        extra = {"median_model_min_bulk_ess": float(ess_m.median()),
+                 "models_rhat_over_1.01": int((rhat_m > 1.01).sum()), "models_rhat_over_1.05": int((rhat_m > 1.05).sum()),
+                 "models": M}
+        picked = list(range(0, M, 64))  # the strided sample the --diagnose comparison runs on the oracle
+        if diagnose:
+            rows = torch.tensor([cpm * m + i for m in picked for i in range(cpm)], device=zd.device)
+            z = zd.index_select(0, rows).cpu().numpy()
+        rhat = [float(rhat_m[m]) for m in picked]
     else:
-        z = out["z"].cpu().numpy()
-    del out
-    if w == "uneven_hier":  # ESS per model over its 4 chains, padding excluded
-        ess, rhat = [], []
-        for i, m in enumerate(picked):
-            e, r = min_bulk_ess(z[4 * i:4 * i + 4, :, :model.chain_latent_dim(4 * m, 4)])
-            ess.append(e)
-            rhat.append(r)
-        ess_min, rhat_max = float(np.min(ess)), float(np.max(rhat))
-        ess_note = "min over a strided sample of 64 models of the per-model min bulk-ESS"
-    elif w in ("sv", "sv_nc"):
-        ess_min, rhat_max = min_bulk_ess(z)
-        ess_note = "min over every 16th step of the walk (h, and h_base when non-centred), nu and s"
-    else:
-        ess_min, rhat_max = min_bulk_ess(z)
-        ess_note = "min over latent coordinates"
+        ess = DD.bulk_effective_sample_size(zd)
+        rhat = DD.split_gelman_rubin(zd)
+        ess_min, rhat_max = float(ess.min()), float(rhat.max())
+        ess_note = "min over latent coordinates, computed on the device"
+        if diagnose:
+            z = zd.cpu().numpy()
+    del out, zd
     grad_evals = float(ns.sum())
     burst, _, hbm, peak_kind = measured_peaks()
     if w == "eight_schools":
@@ -182,7 +200,7 @@ def workload_run(w, precision=None, num_warmup=None, num_samples=None, diagnose=
             "mean_num_steps": float(ns.mean()), "divergences": divergences,
             "min_bulk_ess": ess_min, "min_bulk_ess_per_s_sampling": ess_min / samp_s,
             "min_bulk_ess_per_s_total": ess_min / (warm_s + samp_s), "rhat_max": rhat_max,
-            "ess_definition": ess_note, "ticks_sampling": ticks if ticks else None,
+            "ess_definition": ess_note, **extra, "ticks_sampling": ticks if ticks else None,
             "us_per_tick": 1e6 * samp_s / ticks if ticks else None,
             "engine": "tick engine + CUDA graphs" if ticks else "persistent (one launch)",
             "roofline": roof, "tuning": k.tuning()}

@@ -200,7 +200,11 @@ def summary(samples, prob=0.90, group_by_chain=True):
 
 def print_summary(samples, prob=0.90, group_by_chain=True):
     """diagnostics.py:290-345"""
-    stats = summary(samples, prob, group_by_chain)
+    print_stats(summary(samples, prob, group_by_chain))
+
+
+def print_stats(stats):
+    """The table of print_summary from summary()'s dict (also fed by device_diagnostics.summary)."""
     if not stats:
         return
     first = next(iter(stats.values()))

@@ -62,7 +62,13 @@ class MCMC:
     """MCMC driver with numpyro's constructor (numpyro/infer/mcmc.py:326-393)."""
 
     def __init__(self, sampler, *, num_warmup, num_samples, num_chains=1, thinning=1, postprocess_fn=None,
-                 chain_method="vectorized", progress_bar=False, progress_rate=None, jit_model_args=False):
+                 chain_method="vectorized", progress_bar=False, progress_rate=None, jit_model_args=False,
+                 keep_on_device=False):
+        """keep_on_device (no counterpart in numpyro's constructor): with a GB300 kernel, leave the
+        collected draws in HBM as torch tensors, as numpyro leaves them on the accelerator until
+        transfer_states_to_host (mcmc.py:799-804); print_summary then computes its statistics on the
+        device (device_diagnostics) and only the per-coordinate results move."""
+        self.keep_on_device = bool(keep_on_device)
         self.sampler = sampler
         self._sample_field = sampler.sample_field
         self._default_fields = sampler.default_fields
@@ -185,9 +191,12 @@ class MCMC:
         states = {}
         for f in fields:
             if f in out:
-                v = _to_numpy(out[f])
-                if f == "diverging":
-                    v = v.astype(bool)
+                if self.keep_on_device:
+                    v = out[f].bool() if f == "diverging" else out[f]
+                else:
+                    v = _to_numpy(out[f])
+                    if f == "diverging":
+                        v = v.astype(bool)
                 states[f] = v
             else:
                 states[f] = np.zeros((state.z.shape[0], 0) + ((state.z.shape[1],) if f == "z" else ()))
@@ -225,9 +234,9 @@ class MCMC:
         return out if group_by_chain else {k: self._flat(v) for k, v in out.items()}
 
     def transfer_states_to_host(self):
-        """Collected states as host arrays (mcmc.py:799-804).  The device run already copies its
-        draws to host memory once, at the end; this converts anything still on the device (a
-        postprocess_fn may return tensors).  last_state stays on the device, to resume from."""
+        """Collected states as host arrays (mcmc.py:799-804).  The device run copies its draws to
+        host memory once, at the end, unless keep_on_device; this converts anything still on the
+        device.  last_state stays on the device, to resume from."""
         def conv(x):
             return {k: conv(v) for k, v in x.items()} if isinstance(x, dict) else _to_numpy(x)
 
@@ -242,7 +251,14 @@ class MCMC:
             names = [s.name for s in getattr(getattr(self.sampler, "model", None), "sites", ())]
             if names:
                 sites = {k: v for k, v in sites.items() if k in names}
-        diagnostics.print_summary(sites, prob=prob)
+        leaves = list(sites.values()) if isinstance(sites, dict) else [sites]
+        if leaves and all(hasattr(v, "device") and hasattr(v, "detach") for v in leaves):
+            from . import device_diagnostics
+
+            diagnostics.print_stats(device_diagnostics.summary(sites, prob=prob))
+        else:
+            diagnostics.print_summary(sites, prob=prob)
         extra = self.get_extra_fields()
         if "diverging" in extra:
-            print("Number of divergences: {}".format(int(np.sum(extra["diverging"]))))
+            d = extra["diverging"]
+            print("Number of divergences: {}".format(int(d.sum().item() if hasattr(d, "device") else np.sum(d))))

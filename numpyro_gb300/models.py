@@ -36,6 +36,14 @@ from . import _lib
 Site = namedtuple("Site", ["name", "size", "positive"])
 
 
+
+def _is_tensor(x):
+    return hasattr(x, "detach") and hasattr(x, "device")
+
+
+def _exp(v):
+    return v.exp() if _is_tensor(v) else np.exp(v)
+
 class Model:
     """Base class of registry models (the ``model=`` argument of NUTS/HMC)."""
 
@@ -61,16 +69,17 @@ class Model:
         return out
 
     def postprocess(self, z):
-        """Unconstrained [..., D] -> dict of constrained site values."""
-        z = np.asarray(z)
+        """Unconstrained [..., D] -> dict of constrained site values (numpy arrays, or torch tensors
+        on their own device when z is one: draws kept in HBM stay there)."""
+        z = z if _is_tensor(z) else np.asarray(z)
         out = {}
         for name, (a, b, positive) in self.site_slices().items():
             v = z[..., a:b]
-            out[name] = np.exp(v) if positive else v
+            out[name] = _exp(v) if positive else v
         return out
 
     def unravel(self, z):
-        z = np.asarray(z)
+        z = z if _is_tensor(z) else np.asarray(z)
         return {name: z[..., a:b] for name, (a, b, _) in self.site_slices().items()}
 
 
@@ -202,7 +211,8 @@ class StochasticVolatility(Model):
     def postprocess(self, z):
         out = super().postprocess(z)
         if self.noncentered:
-            out["h"] = out["s"] * np.cumsum(out["h_base"], axis=-1)
+            hb = out["h_base"]
+            out["h"] = out["s"] * (hb.cumsum(dim=-1) if _is_tensor(hb) else np.cumsum(hb, axis=-1))
         return out
 
     def descriptor(self):

@@ -88,3 +88,55 @@ def test_posterior_gate_bounds():
     b3, bound = mod.moment_bounds(110)
     ok = (np.sum(z > 3, axis=1) <= b3) & (z.max(axis=1) <= bound)
     assert ok.mean() > 0.97
+
+
+def _ar1_draws_with_ties(C, S, K, seed=0):
+    rng = np.random.default_rng(seed)
+    x = np.zeros((C, S, K))
+    e = rng.standard_normal((C, S, K))
+    for s in range(S):
+        x[:, s] = 0.6 * x[:, s - 1] + e[:, s] if s else e[:, s]
+    stay = rng.random((C, S)) < 0.2  # rejected transitions repeat their draw
+    for c in range(C):
+        for s in range(1, S):
+            if stay[c, s]:
+                x[c, s] = x[c, s - 1]
+    x[:, :, 3] = np.round(x[:, :, 3])  # a coordinate of heavy ties
+    return x
+
+
+def test_device_diagnostics_equal_the_host_estimators():
+    """device_diagnostics (torch, here on CPU tensors: the same code runs on the GPU) against the
+    host restatement of numpyro's estimators, with ties and in chunks that split the coordinates."""
+    torch = pytest.importorskip("torch")
+    from numpyro_gb300 import device_diagnostics as DD
+    from numpyro_gb300 import diagnostics as D
+
+    x = _ar1_draws_with_ties(8, 301, 37)
+    t = torch.as_tensor(x)
+    for name in ("split_gelman_rubin", "gelman_rubin", "effective_sample_size", "bulk_effective_sample_size",
+                 "mcse_mean", "mcse_sd"):
+        a, b = getattr(D, name)(x), getattr(DD, name)(t, chunk=10).numpy()
+        np.testing.assert_allclose(b, a, rtol=1e-12, err_msg=name)
+    np.testing.assert_allclose(DD.rank_normalize(t, chunk=7).numpy(), D.rank_normalize(x), atol=1e-12)
+    hs, ds = D.summary({"a": x}), DD.summary({"a": t})
+    for k in hs["a"]:
+        np.testing.assert_allclose(ds["a"][k], np.asarray(hs["a"][k]), rtol=1e-12, atol=1e-14, err_msg=k)
+    st = DD.summary_stats(t, chunk=9)
+    np.testing.assert_allclose(st["bulk_ess"].numpy(), D.bulk_effective_sample_size(x), rtol=1e-12)
+    np.testing.assert_allclose(st["r_hat"].numpy(), D.split_gelman_rubin(x), rtol=1e-12)
+
+
+def test_device_diagnostics_on_a_model_major_view():
+    """Per-model statistics of a batch of models without copying the draws: the chains of model m
+    are rows 4m..4m+3, viewed as [4 chains, draws, models, coordinates]."""
+    torch = pytest.importorskip("torch")
+    from numpyro_gb300 import device_diagnostics as DD
+    from numpyro_gb300 import diagnostics as D
+
+    y = _ar1_draws_with_ties(6 * 4, 120, 5, seed=3)
+    yt = torch.as_tensor(y).view(6, 4, 120, 5).permute(1, 2, 0, 3)
+    ref = np.stack([D.bulk_effective_sample_size(y[4 * m:4 * m + 4]) for m in range(6)])
+    np.testing.assert_allclose(DD.bulk_effective_sample_size(yt, chunk=7).numpy(), ref, rtol=1e-12)
+    ref = np.stack([D.split_gelman_rubin(y[4 * m:4 * m + 4]) for m in range(6)])
+    np.testing.assert_allclose(DD.split_gelman_rubin(yt, chunk=3).numpy(), ref, rtol=1e-12)

@@ -48,6 +48,36 @@ def test_mcmc_api_eight_schools():
 
 
 @pytest.mark.gpu
+def test_mcmc_keeps_draws_on_the_device_and_summarises_them_there(capsys):
+    """keep_on_device=True: the same draws as the host-copy run, as CUDA tensors; print_summary's
+    statistics (device_diagnostics) equal the host ones; transfer_states_to_host moves them."""
+    from numpyro_gb300 import device_diagnostics as DD
+    from numpyro_gb300 import diagnostics as D
+
+    y, s = datasets.eight_schools(0)
+    model = models.HierarchicalNormal(y, s)
+    host = MCMC(NUTS(model), num_warmup=200, num_samples=300, num_chains=4)
+    host.run(3)
+    dev = MCMC(NUTS(model), num_warmup=200, num_samples=300, num_chains=4, keep_on_device=True)
+    dev.run(3)
+    hs, ds = host.get_samples(group_by_chain=True), dev.get_samples(group_by_chain=True)
+    for k in hs:
+        assert ds[k].is_cuda, k
+        # the same unconstrained draws; exp of the positive sites by the device's own exp
+        np.testing.assert_allclose(ds[k].cpu().numpy(), hs[k], rtol=1e-6, atol=1e-7, err_msg=k)
+    assert dev.get_extra_fields()["diverging"].dtype == torch.bool
+    a, b = D.summary({k: ds[k].cpu().numpy() for k in ds}), DD.summary(ds)
+    for site in a:
+        for stat in a[site]:
+            np.testing.assert_allclose(b[site][stat], np.asarray(a[site][stat]), rtol=1e-9, atol=1e-9,
+                                       err_msg="%s %s" % (site, stat))
+    dev.print_summary()
+    assert "theta_base" in capsys.readouterr().out
+    dev.transfer_states_to_host()
+    assert isinstance(dev.get_samples()["mu"], np.ndarray)
+
+
+@pytest.mark.gpu
 def test_eight_schools_posterior_matches_oracle():
     y, s = datasets.eight_schools(0)
     model = models.HierarchicalNormal(y, s)
