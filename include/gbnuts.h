@@ -32,7 +32,7 @@
 extern "C" {
 #endif
 
-#define GBN_ABI_VERSION 1
+#define GBN_ABI_VERSION 2
 
 /* status codes */
 #define GBN_OK 0
@@ -106,6 +106,12 @@ typedef struct {
   double max_delta_energy;  /* 1000 */
   double init_step_size;
   uint64_t seed;
+  /* Block-structured mass matrices (numpyro's dense_mass as a list of site-name tuples,
+   * hmc_util.py:439-486), with dense_mass = 1: NULL, or latent-dim entries, the dense block of
+   * each coordinate (>= 0) or -1 for the coordinates the remaining diagonal block holds.  The
+   * mass matrices stay [C][D][D] (block-diagonal); at each window end the Welford covariance keeps
+   * only the entries within a block and the diagonal. */
+  const int32_t* mass_blocks;
 } gbn_config;
 
 /* HMCState (numpyro/infer/hmc.py:31-47) + HMCAdaptState (hmc_util.py:18-30)

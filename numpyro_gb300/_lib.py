@@ -66,6 +66,7 @@ class Config(ctypes.Structure):
         ("max_delta_energy", ctypes.c_double),
         ("init_step_size", ctypes.c_double),
         ("seed", ctypes.c_uint64),
+        ("mass_blocks", c_int32_p),
     ]
 
 

@@ -364,6 +364,21 @@ int gbn_create(gbn_handle* out, const gbn_model_desc* md, const gbn_config* cfg)
     return fail(nullptr, GBN_ERR_UNSUPPORTED,
                 "dense_mass=True needs a latent dimension <= 1024 (a warp per chain; not the SV family)");
   }
+  if (cfg->mass_blocks && !cfg->dense_mass) {
+    gbn_destroy(h);
+    return fail(nullptr, GBN_ERR_INVALID_ARG, "mass_blocks needs dense_mass = 1");
+  }
+  if (cfg->mass_blocks) {
+    for (int d = 0; d < D; ++d)
+      if (cfg->mass_blocks[d] < -1) {
+        gbn_destroy(h);
+        return fail(nullptr, GBN_ERR_INVALID_ARG, "mass_blocks entries must be >= -1");
+      }
+    int32_t* mb = nullptr;
+    if (ce == cudaSuccess) ce = dalloc(h, &mb, (size_t)D);
+    if (ce == cudaSuccess) ce = cudaMemcpy(mb, cfg->mass_blocks, sizeof(int32_t) * D, cudaMemcpyHostToDevice);
+    h->hp.mass_block = mb;
+  }
   if (ce == cudaSuccess && cfg->dense_mass) ce = dalloc(h, &e.tmp, CD);
   if (ce == cudaSuccess && cfg->dense_mass) ce = dalloc(h, &e.tmpd, 2 * CD);
   if (ce == cudaSuccess) ce = dalloc(h, &e.r_ck, CD * h->maxd);

@@ -264,6 +264,7 @@ struct __align__(16) AdvParams {
   int32_t adapt_step, adapt_mass, regularize, heuristic;
   int32_t lockstep;
   int32_t dense;  // mass matrices [C][D][D] (dense_mass=True) instead of [C][D]
+  const int32_t* mass_block;  // [D] dense block of each coordinate, -1 diagonal; null: one dense block
   int32_t fixed_steps;
   int32_t collect_start, thinning, num_collect;
   float target_accept;

@@ -652,10 +652,12 @@ struct Chain {
         const double shrink = P.regularize ? 1e-3 * (5.0 / (nn + 5.0)) : 0.0;
         const double inv_nm1 = 1.0 / (double)(nn - 1);
         g.sync();
+        const int32_t* blk = P.mass_block;  // block-structured: entries across blocks are zero
         for (int j = g.tid; j < D; j += NT)
           for (int i = 0; i < D; ++i) {
             const size_t o = (size_t)i * ld + j;
-            m2[o] = a * (m2[o] * inv_nm1) + (i == j ? shrink : 0.0);
+            const bool keep = !blk || i == j || (blk[i] >= 0 && blk[i] == blk[j]);
+            m2[o] = keep ? a * (m2[o] * inv_nm1) + (i == j ? shrink : 0.0) : 0.0;
           }
         dense_factor(g, m2, D, ld, MX(P.s.inverse_mass_matrix), MX(P.s.mass_matrix_sqrt),
                      MX(P.s.mass_matrix_sqrt_inv));

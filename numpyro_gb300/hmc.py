@@ -62,6 +62,29 @@ def _ptr(t, ctype):
     return ctypes.cast(ctypes.c_void_p(t.data_ptr()), ctype)
 
 
+
+def mass_blocks_of(model, dense_mass):
+    """numpyro's block-structured dense_mass (a list of tuples of site names,
+    numpyro/infer/hmc_util.py:439-486: each tuple a dense block over its sites, the sites in no
+    tuple one diagonal block) as the engine's per-coordinate block ids: the tuple's index for its
+    sites' coordinates, -1 for the rest."""
+    slices = model.site_slices()
+    blocks = np.full(model.latent_dim, -1, np.int32)
+    seen = set()
+    for b, names in enumerate(dense_mass):
+        if isinstance(names, str) or not isinstance(names, (tuple, list)):
+            raise ValueError("dense_mass blocks must be tuples of site names, got %r" % (names,))
+        for name in names:
+            if name not in slices:
+                raise ValueError("dense_mass names site %r, which the model does not have (%s)"
+                                 % (name, ", ".join(sorted(slices))))
+            if name in seen:
+                raise ValueError("site %r is in more than one dense_mass block" % (name,))
+            seen.add(name)
+            a, e, _ = slices[name]
+            blocks[a:e] = b
+    return blocks
+
 class HMC(MCMCKernel):
     """Hamiltonian Monte Carlo with fixed trajectory length (numpyro/infer/hmc.py:541-822).
 
@@ -87,10 +110,12 @@ class HMC(MCMCKernel):
             raise NotImplementedError("model must be a numpyro_gb300.models registry model")
         if kinetic_fn is not None:
             raise NotImplementedError("only the Euclidean kinetic energy is supported")
-        if dense_mass not in (False, True, [], None):
-            # numpyro also takes a list of site-name tuples (block-structured mass matrices)
-            raise NotImplementedError("dense_mass must be True or False (block-structured mass matrices are not "
-                                      "supported by this engine)")
+        self._mass_blocks = None
+        if isinstance(dense_mass, list) and dense_mass:
+            self._mass_blocks = mass_blocks_of(model, dense_mass)
+            dense_mass = True
+        elif dense_mass not in (False, True, [], None):
+            raise ValueError("dense_mass must be a bool or a list of tuples of site names")
         if init_strategy is not init_to_uniform:
             raise NotImplementedError("only init_to_uniform(radius=2) runs on the device")
         if type(self) is HMC:
@@ -164,6 +189,8 @@ class HMC(MCMCKernel):
         cfg.adapt_step_size = int(bool(self._adapt_step_size))
         cfg.adapt_mass_matrix = int(bool(self._adapt_mass_matrix))
         cfg.dense_mass = int(self._dense_mass)
+        if self._mass_blocks is not None:
+            cfg.mass_blocks = self._mass_blocks.ctypes.data_as(_lib.c_int32_p)  # read at gbn_create
         cfg.regularize_mass_matrix = int(bool(self._regularize_mass_matrix))
         cfg.find_heuristic_step_size = int(bool(self._find_heuristic_step_size))
         cfg.num_steps = int(self._num_steps or 0)

@@ -29,7 +29,7 @@ def test_library_loads_and_exports_every_declared_symbol():
     lib = ctypes.CDLL(_lib.LIB_PATH)
     for s in _declared_symbols():
         assert hasattr(lib, s), s
-    assert lib.gbn_abi_version() == 1
+    assert lib.gbn_abi_version() == 2
 
 
 def test_struct_layouts_match_header():
@@ -66,8 +66,20 @@ def test_kernel_constructor_contract():
     with pytest.raises(NotImplementedError):
         NUTS(potential_fn=lambda z: z)
     assert NUTS(m, dense_mass=True)._dense_mass
-    with pytest.raises(NotImplementedError):  # block-structured dense mass
-        NUTS(m, dense_mass=[("mu", "tau")])
+    # block-structured dense mass (numpyro's list of site tuples): per-coordinate block ids
+    k = NUTS(m, dense_mass=[("theta_base", "mu")])
+    assert k._dense_mass
+    sl = m.site_slices()
+    expect = np.full(m.latent_dim, -1, np.int32)
+    expect[sl["mu"][0]:sl["mu"][1]] = 0
+    expect[sl["theta_base"][0]:sl["theta_base"][1]] = 0
+    np.testing.assert_array_equal(k._mass_blocks, expect)
+    k = NUTS(m, dense_mass=[("mu",), ("tau", "theta_base")])
+    assert list(k._mass_blocks[:2]) == [0, 1] and set(k._mass_blocks[2:]) == {1}
+    assert not NUTS(m, dense_mass=[])._dense_mass
+    for bad in ([("mu", "nope")], [("mu",), ("mu", "tau")], ["mu"], "mu"):
+        with pytest.raises(ValueError):
+            NUTS(m, dense_mass=bad)
     with pytest.raises(ValueError):
         HMC(m, num_steps=None, trajectory_length=None)
 

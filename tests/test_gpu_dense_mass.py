@@ -129,3 +129,72 @@ def test_dense_mass_mcmc_matches_diagonal_posterior():
         mcse = np.sqrt(a.std(axis=(0, 1)) ** 2 / e1 + b.std(axis=(0, 1)) ** 2 / e2)
         assert np.all(np.abs(m1 - m2) <= 4 * mcse), (site, m1, m2, mcse)
         assert np.all(diagnostics.split_gelman_rubin(a) < 1.05)
+
+
+@pytest.mark.gpu
+def test_block_structured_window_end_matches_numpyro_blocks():
+    """dense_mass=[("theta_base", "mu")] (numpyro's list form, hmc_util.py:439-486): one dense block
+    over theta_base and mu -- listed out of the sites' order, with tau between them in z -- and
+    tau in the remaining diagonal block.  At the window end the device's inverse mass matrix is
+    the oracle's welford final_fn of each block (dense for the tuple, diagonal for the rest) in
+    the full coordinates and zero across blocks, and its square roots reproduce M^-1 and M."""
+    model, _ = _hier()
+    D = model.latent_dim
+    sl = model.site_slices()
+    blockA = list(range(*sl["theta_base"][:2])) + list(range(*sl["mu"][:2]))  # the tuple's order
+    diag = list(range(*sl["tau"][:2]))
+    C, W = 8, 200
+    sched = R.build_adaptation_schedule(W)
+    t_end = sched[1].end
+    k = NUTS(model, num_chains=C, dense_mass=[("theta_base", "mu")])
+    st = k.init(SEED, W)
+    rng = np.random.default_rng(5)
+    n0 = sched[1].end - sched[1].start
+    mean0 = rng.standard_normal((C, D))
+    X = rng.standard_normal((C, n0, D)) @ np.linalg.cholesky(_spd(D, 3).astype(np.float64)).T
+    m20 = np.einsum("cni,cnj->cij", X - X.mean(1, keepdims=True), X - X.mean(1, keepdims=True))
+    a = st.adapt_state
+    st.i.fill_(t_end)
+    a.window_idx.fill_(1)
+    a.mm_state[0].copy_(torch.as_tensor(mean0, device="cuda"))
+    a.mm_state[1].copy_(torch.as_tensor(m20, device="cuda"))
+    a.mm_state[2].fill_(n0)
+    new = k.sample(st)
+    zn = new.z.double().cpu().numpy()
+    na = new.adapt_state
+    _, upd_d, fin_d = R.welford_covariance(diagonal=False)
+    _, upd_v, fin_v = R.welford_covariance(diagonal=True)
+    for c in range(C):
+        inv = na.inverse_mass_matrix[c].double().cpu().numpy()
+        sq = na.mass_matrix_sqrt[c].double().cpu().numpy()
+        sqi = na.mass_matrix_sqrt_inv[c].double().cpu().numpy()
+        ia = np.ix_(blockA, blockA)
+        mm = upd_d(zn[c][blockA], (mean0[c][blockA], m20[c][ia], n0))
+        covA, _, _ = fin_d(mm, regularize=True)
+        mv = upd_v(zn[c][diag], (mean0[c][diag], np.diag(m20[c])[diag], n0))
+        varD, _, _ = fin_v(mv, regularize=True)
+        expect = np.zeros((D, D))
+        expect[ia] = covA
+        expect[diag, diag] = varD
+        np.testing.assert_allclose(inv, expect, rtol=1e-5, atol=1e-7)
+        # numpyro's factors: mass_matrix_sqrt_inv^T mass_matrix_sqrt_inv = M^-1, sqrt sqrt^T = M
+        np.testing.assert_allclose(sqi.T @ sqi, expect, rtol=2e-5, atol=2e-6)
+        np.testing.assert_allclose(sq @ sq.T, np.linalg.inv(expect), rtol=2e-4, atol=2e-5)
+        assert np.all(sq[np.ix_(diag, blockA)] == 0) and np.all(sq[np.ix_(blockA, diag)] == 0)
+    k.close()
+
+
+@pytest.mark.gpu
+def test_block_structured_mass_mcmc_matches_diagonal_posterior():
+    model, _ = _hier()
+    res = {}
+    for dense in (False, [("mu", "tau")]):
+        mcmc = MCMC(NUTS(model, dense_mass=dense), num_warmup=400, num_samples=600, num_chains=16)
+        mcmc.run(8)
+        res[bool(dense)] = mcmc.get_samples(group_by_chain=True)
+    for site in ("mu", "tau"):
+        a, b = res[True][site].reshape(16, 600, -1), res[False][site].reshape(16, 600, -1)
+        m1, m2 = a.mean(axis=(0, 1)), b.mean(axis=(0, 1))
+        mcse = np.sqrt(diagnostics.mcse_mean(a) ** 2 + diagnostics.mcse_mean(b) ** 2)
+        assert np.all(np.abs(m1 - m2) <= 4 * mcse), (site, m1, m2, mcse)
+        assert np.all(diagnostics.split_gelman_rubin(a) < 1.05)
