@@ -64,9 +64,10 @@ def test_mcmc_keeps_draws_on_the_device_and_summarises_them_there(capsys):
     for k in hs:
         assert ds[k].is_cuda, k
         # the same unconstrained draws; exp of the positive sites by the device's own exp
-        np.testing.assert_allclose(ds[k].cpu().numpy(), hs[k], rtol=1e-6, atol=1e-7, err_msg=k)
+        # (theta = mu + tau theta_base cancels: an ulp of tau's exp shows as ~1e-6 absolute)
+        np.testing.assert_allclose(ds[k].cpu().numpy(), hs[k], rtol=1e-5, atol=1e-5, err_msg=k)
     assert dev.get_extra_fields()["diverging"].dtype == torch.bool
-    a, b = D.summary({k: ds[k].cpu().numpy() for k in ds}), DD.summary(ds)
+    a, b = D.summary({k: ds[k].cpu().double().numpy() for k in ds}), DD.summary(ds)  # both in FP64
     for site in a:
         for stat in a[site]:
             np.testing.assert_allclose(b[site][stat], np.asarray(a[site][stat]), rtol=1e-9, atol=1e-9,
