@@ -155,10 +155,11 @@ def workload_run(w, precision=None, num_warmup=None, num_samples=None, diagnose=
                  "models_rhat_over_1.01": int((rhat_m > 1.01).sum()), "models_rhat_over_1.05": int((rhat_m > 1.05).sum()),
                  "models": M}
         picked = list(range(0, M, 64))  # the strided sample the --diagnose comparison runs on the oracle
+        worst = [int(m) for m in torch.argsort(rhat_m, descending=True)[:4].tolist()]  # and the GPU's worst
         if diagnose:
-            rows = torch.tensor([cpm * m + i for m in picked for i in range(cpm)], device=zd.device)
+            rows = torch.tensor([cpm * m + i for m in picked + worst for i in range(cpm)], device=zd.device)
             z = zd.index_select(0, rows).cpu().numpy()
-        rhat = [float(rhat_m[m]) for m in picked]
+        rhat = worst
     else:
         ess = DD.bulk_effective_sample_size(zd)
         rhat = DD.split_gelman_rubin(zd)
@@ -224,7 +225,21 @@ def _oracle_diagnosis(w, model, z, picked, W, S, model_rhat):
                      "%d samples, %d host threads" % (W, S, cores)}
     if w == "uneven_hier":
         # every model of the strided sample, 4 chains each with the GPU's chain ids and stream: the
-        # distribution of per-model R-hat and ESS under numpyro's algorithm beside the GPU's
+        # distribution of per-model R-hat and ESS under numpyro's algorithm beside the GPU's; then
+        # the GPU's four worst models of all (model_rhat: their ids; their draws follow in z)
+        worst_rows = []
+        for i, m in enumerate(model_rhat or []):
+            D = model.chain_latent_dim(4 * m, 4)
+            res = build_oracle.run_model(lib, cm, model.latent_dim, 4, W, S, seed=1, first_chain=4 * m,
+                                         threads=min(cores, 4))
+            e_o, r_o = min_bulk_ess(res["samples"][:, :, :D])
+            k = len(picked) + i
+            e_g, r_g = min_bulk_ess(z[4 * k:4 * k + 4, :, :D])
+            worst_rows.append({"model": int(m), "J": D - 2, "gpu_rhat": r_g, "oracle_rhat": r_o, "gpu_min_bulk_ess": e_g,
+                               "oracle_min_bulk_ess": e_o, "oracle_divergences": int(res["diverging"].sum()),
+                               "gpu_chain_sds_of_log_tau": [float(np.std(z[4 * k + j, :, 1])) for j in range(4)],
+                               "oracle_chain_sds_of_log_tau": [float(np.std(res["samples"][j, :, 1])) for j in range(4)]})
+        out["gpu_worst_models_of_all"] = worst_rows
         g_r, g_e, o_r, o_e, o_div, rows = [], [], [], [], 0, []
         for i, m in enumerate(picked):
             D = model.chain_latent_dim(4 * m, 4)
