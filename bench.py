@@ -140,14 +140,7 @@ def workload_run(w, precision=None, num_warmup=None, num_samples=None, diagnose=
             z = zd.index_select(2, idx).cpu().numpy()
     elif w == "uneven_hier":
         M, cpm = model.num_models, C // model.num_models
-        Dmax = zd.shape[-1]
-        zm = zd.view(M, cpm, zd.shape[1], Dmax).permute(1, 2, 0, 3)  # [chains of a model, draws, model, coord]
-        ess = DD.bulk_effective_sample_size(zm, chunk=4096)
-        rhat = DD.split_gelman_rubin(zm, chunk=4096)
-        dims = torch.tensor([model.chain_latent_dim(cpm * m, cpm) for m in range(M)], device=zd.device)
-        valid = torch.arange(Dmax, device=zd.device)[None, :] < dims[:, None]  # padding excluded
-        ess_m = torch.where(valid, torch.nan_to_num(ess, nan=float("inf")), torch.full_like(ess, float("inf"))).min(dim=1).values
-        rhat_m = torch.where(valid, torch.nan_to_num(rhat), torch.zeros_like(rhat)).max(dim=1).values
+        ess_m, rhat_m = per_model_diagnostics(zd, M, cpm, [model.chain_latent_dim(cpm * m, cpm) for m in range(M)])
         ess_min, rhat_max = float(ess_m.min()), float(rhat_m.max())
         ess_note = "min over all %d models of the per-model min bulk-ESS (its %d chains), computed on the device" % (
             M, cpm)
@@ -374,6 +367,25 @@ class Clocks:
                     reasons.add(nm)
         med = float(np.median(sm)) if sm else None
         return {"sm_mhz": med, "sm_max_mhz": smax, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def per_model_diagnostics(zd, num_models, chains_per_model, dims, chunk=4096):
+    """Per-model min bulk-ESS and max split R-hat of a batch of models' draws zd [models x chains,
+    draws, padded dim] (model m's chains are rows m * chains_per_model ...), over each model's own
+    dims[m] coordinates, on zd's device without copying the draws (a model-major view)."""
+    import torch
+
+    from numpyro_gb300 import device_diagnostics as DD
+
+    M, cpm, Dmax = num_models, chains_per_model, zd.shape[-1]
+    zm = zd.view(M, cpm, zd.shape[1], Dmax).permute(1, 2, 0, 3)  # [chains of a model, draws, model, coord]
+    ess = DD.bulk_effective_sample_size(zm, chunk=chunk)
+    rhat = DD.split_gelman_rubin(zm, chunk=chunk)
+    d = torch.as_tensor(dims, device=zd.device)
+    valid = torch.arange(Dmax, device=zd.device)[None, :] < d[:, None]  # padding excluded
+    ess_m = torch.where(valid, torch.nan_to_num(ess, nan=float("inf")), torch.full_like(ess, float("inf")))
+    rhat_m = torch.where(valid, torch.nan_to_num(rhat), torch.zeros_like(rhat))
+    return ess_m.min(dim=1).values, rhat_m.max(dim=1).values
 
 
 def min_bulk_ess(z):

@@ -1,9 +1,13 @@
 """bench.py's host side on CPU: the reference arm's JSON line (its timed CPU leg stubbed), the clock
-sampler's fallback without nvidia-smi, and the launch count per tick."""
+sampler's fallback without nvidia-smi, the launch count per tick, and the per-model diagnostics of
+the uneven hierarchical workload."""
 import importlib.util
 import json
 import os
 import types
+
+import numpy as np
+import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
@@ -53,3 +57,22 @@ def test_launches_per_tick():
     b = _bench()
     assert b._launches_per_tick("bf16x3") == 2  # advance (with split and finish fused), tensor-core potential
     assert b._launches_per_tick("fp32") == 3    # advance, CUDA-core potential, finish
+
+
+def test_per_model_diagnostics_match_the_host_estimators():
+    """bench.py's per-model ESS / R-hat over a batch of uneven models (model-major view of the
+    draws, each model's padding excluded) against the host estimators model by model."""
+    torch = pytest.importorskip("torch")
+    from numpyro_gb300 import diagnostics as D
+
+    rng = np.random.default_rng(2)
+    M, cpm, S, Dmax = 5, 4, 80, 7
+    dims = [7, 3, 5, 2, 6]
+    z = rng.standard_normal((M * cpm, S, Dmax)).cumsum(axis=1) * 0.2 + rng.standard_normal((M * cpm, S, Dmax))
+    for m, d in enumerate(dims):
+        z[m * cpm:(m + 1) * cpm, :, d:] = 0.0  # padding
+    ess_m, rhat_m = _bench().per_model_diagnostics(torch.as_tensor(z), M, cpm, dims, chunk=6)
+    for m, d in enumerate(dims):
+        zz = z[m * cpm:(m + 1) * cpm, :, :d]
+        np.testing.assert_allclose(float(ess_m[m]), D.bulk_effective_sample_size(zz).min(), rtol=1e-10)
+        np.testing.assert_allclose(float(rhat_m[m]), D.split_gelman_rubin(zz).max(), rtol=1e-10)
