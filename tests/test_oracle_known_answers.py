@@ -225,3 +225,44 @@ def test_build_tree(step_size, seed):
         assert tree.num_proposals == 1
     if step_size < 0.1:
         assert tree.num_proposals > 10
+
+
+def test_masked_dense_welford_is_numpyros_block_structured_mass():
+    """The engine's block-structured mass (dense Welford over all coordinates, then only in-block
+    entries and the diagonal kept) equals numpyro's per-block adaptation (hmc_util.py:439-486: a
+    dense welford_covariance per listed block, a diagonal one for the rest), and the reverse
+    Cholesky factors of that block-diagonal matrix have no fill-in, with blocks interleaved in the
+    coordinates and a block listed out of coordinate order."""
+    rng = np.random.RandomState(1)
+    D, n = 7, 400
+    a = rng.randn(D, D)
+    x = rng.multivariate_normal(rng.randn(D), a @ a.T + np.eye(D), size=n)
+    blocks = [[5, 1, 3], [0, 6]]  # tuple order as listed; coordinates 2 and 4 in the diagonal block
+    rest = [2, 4]
+    full = R.welford_covariance(diagonal=False)
+    st = full[0](D)
+    for i in range(n):
+        st = full[1](x[i], st)
+    cov_full, _, _ = full[2](st, regularize=True)
+    keep = np.eye(D, dtype=bool)
+    for b in blocks:
+        keep[np.ix_(b, b)] = True
+    masked = np.where(keep, cov_full, 0.0)
+    expect = np.zeros((D, D))
+    for b in blocks:
+        dense = R.welford_covariance(diagonal=False)
+        sb = dense[0](len(b))
+        for i in range(n):
+            sb = dense[1](x[i][b], sb)
+        expect[np.ix_(b, b)], _, _ = dense[2](sb, regularize=True)
+    diag = R.welford_covariance(diagonal=True)
+    sd = diag[0](len(rest))
+    for i in range(n):
+        sd = diag[1](x[i][rest], sd)
+    expect[rest, rest], _, _ = diag[2](sd, regularize=True)
+    assert_allclose(masked, expect, rtol=1e-12, atol=1e-14)
+    # the factors final_fn forms from a covariance equal to the masked matrix (m2 = cov (n - 1))
+    _, sq, sqi = full[2]((np.zeros(D), masked * (n - 1), n), regularize=False)
+    assert np.all(sq[~keep] == 0.0) and np.all(sqi[~keep] == 0.0)
+    assert_allclose(sqi.T @ sqi, masked, rtol=1e-10, atol=1e-12)
+    assert_allclose(sq @ sq.T, np.linalg.inv(masked), rtol=1e-9, atol=1e-10)
