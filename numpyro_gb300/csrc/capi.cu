@@ -59,7 +59,7 @@ struct gbn_handle_s {
   cudaGraphExec_t async_graph = nullptr;
   int32_t* async_iter = nullptr;  // [2]: loop iterations done, iteration budget
   void* async_scratch = nullptr;  // potential scratch the async graph was built with
-  int fuse_tick = 1;              // GBN_FUSE_TICK=0: the tensor-core logistic potential runs unfused
+  int fuse_tick = 1;              // GBN_FUSE_TICK=0: the tensor-core potentials' split and finish run unfused
 };
 
 // The tick engine fuses the tensor-core logistic potential's coefficient split and row-group finish
@@ -73,6 +73,17 @@ static void refresh_fusion(gbn_handle h) {
   P.lrf_bsplit = nullptr;
   P.lrf_split3 = nullptr;
   P.lrf_e_tanh = 0;
+  P.hsf_part_gb = nullptr;
+  P.hsf_part_rr = nullptr;
+  P.hsf_bs = nullptr;
+  // the horseshoe's fused split and finish live in the CTA-per-chain state machine: with a latent
+  // dimension <= 1024 the warp-per-chain kernel runs (launch_advance), and the separate kernels stay
+  const bool cta_engine = h->cta_per_chain || h->D > 1024;
+  if (h->fuse_tick && cta_engine && !h->persistent && h->m.family == GBN_FAMILY_HORSESHOE &&
+      h->m.precision == GBN_PREC_BF16X3 && h->m.hs_tc && !horseshoe_tc_fusion(h->m, h->C, &P)) {
+    P.hsf_part_gb = nullptr;
+    P.hsf_bs = nullptr;
+  }
   if (h->fuse_tick && !h->persistent && h->m.family == GBN_FAMILY_LOGREG && h->m.precision == GBN_PREC_BF16X3 &&
       h->m.tc && !logreg_tc_fusion(h->m, h->C, &P))
     P.lrf_part_g = nullptr;
@@ -420,7 +431,7 @@ int gbn_create(gbn_handle* out, const gbn_model_desc* md, const gbn_config* cfg)
   {
     const char* g = getenv("GBN_CUDA_GRAPHS");  // "0" launches every tick directly
     h->use_graphs = !(g && g[0] == '0');
-    const char* f = getenv("GBN_FUSE_TICK");  // "0": the tensor-core logistic potential's split and finish
+    const char* f = getenv("GBN_FUSE_TICK");  // "0": the tensor-core potentials' split and finish
     h->fuse_tick = !(f && f[0] == '0');       // run as their own kernels
   }
   if (ce == cudaSuccess && m.family == GBN_FAMILY_LOGREG && m.precision == GBN_PREC_BF16X3) {
@@ -542,7 +553,7 @@ static cudaError_t launch_tick_batch(gbn_handle h, cudaStream_t st) {
     const int parity = k & 1;
     launch_advance(h->dP, h->C, h->D, h->cta_per_chain, h->hp.dense != 0, parity, st);
     cudaError_t e = launch_potential(h->m, h->e.Q, h->C, h->e.PE, h->e.G, h->counters + 2 * parity, st,
-                                     h->hp.lrf_part_g != nullptr);
+                                     h->hp.lrf_part_g != nullptr || h->hp.hsf_part_gb != nullptr);
     if (e != cudaSuccess) return e;
   }
   return cudaSuccess;
@@ -867,7 +878,7 @@ int gbn_time_potential(gbn_handle h, void* stream, int32_t reps, float* ms) {
   if (!h || !ms || reps < 1) return fail(h, GBN_ERR_INVALID_ARG, "gbn_time_potential: bad argument");
   cudaStream_t s = (cudaStream_t)stream;
   refresh_fusion(h);
-  const bool fused = h->hp.lrf_part_g != nullptr;
+  const bool fused = h->hp.lrf_part_g != nullptr || h->hp.hsf_part_gb != nullptr;
   cudaEvent_t a = nullptr, b = nullptr;
   cudaError_t e = cudaEventCreate(&a);
   if (e == cudaSuccess) e = cudaEventCreate(&b);

@@ -286,6 +286,16 @@ struct __align__(16) AdvParams {
   int32_t lrf_row_groups;
   const int32_t* lrf_split3;  // per 128-chain block: 1 if the launch took three coefficient terms
   int32_t lrf_e_tanh;         // GEMM2 summed tanh(l'/2) X' (see lr_finish.cuh)
+  // The tensor-core horseshoe potential fused into the tick engine's CTA-per-chain state machine
+  // (hsf_part_gb null: not fused): it finishes the previous tick's potential for the chains that
+  // queried it (hs_finish.cuh) and writes the bf16 hi/mid/lo terms of the coefficients of every
+  // position it queries (what split_beta_kernel does).
+  const float* hsf_part_gb;
+  const double* hsf_part_rr;
+  uint16_t* hsf_bs;  // [3][hsf_total] bfloat16 bits: point c, feature k at c * hsf_kp + k
+  int64_t hsf_N;
+  int64_t hsf_total;
+  int32_t hsf_P, hsf_kp, hsf_splits, hsf_ldg, hsf_ld_rr, hsf_mtiles, hsf_nc, hsf_pad;
 };
 
 // ---------------------------------------------------------------- groups

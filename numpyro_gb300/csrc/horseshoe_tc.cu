@@ -377,6 +377,8 @@ cudaError_t horseshoe_tc_prepare(ModelDev& m, int points) {
     e = cudaMalloc(&s->xs, sizeof(__nv_bfloat16) * nx);
     if (e == cudaSuccess) e = cudaMalloc(&s->xts, sizeof(__nv_bfloat16) * nxt);
     if (e == cudaSuccess) e = cudaMalloc(&s->bs, sizeof(__nv_bfloat16) * 3 * (size_t)s->cp * s->kp);
+    // padding (features k >= p, points c >= npts) stays zero: the fused tick writes only real entries
+    if (e == cudaSuccess) e = cudaMemset(s->bs, 0, sizeof(__nv_bfloat16) * 3 * (size_t)s->cp * s->kp);
     if (e == cudaSuccess) e = cudaMalloc(&s->rts, sizeof(__nv_bfloat16) * 3 * (size_t)s->cp * s->np);
     if (e == cudaSuccess) e = cudaMalloc(&s->part_gb, sizeof(float) * (size_t)s->splits * s->cp * s->pp);
     if (e == cudaSuccess) e = cudaMalloc(&s->part_rr, sizeof(double) * (size_t)(s->np / TN) * s->cp);
@@ -429,16 +431,39 @@ void horseshoe_finish_launch(const float* Q, int npts, int ld, int P, int64_t N,
                              int ldg, const double* part_rr, int ld_rr, int mtiles, int noncentred, double* PE,
                              float* G, const int32_t* pending, cudaStream_t st);
 
+bool horseshoe_tc_fusion(ModelDev& m, int npts, AdvParams* P) {
+  using namespace hstc;
+  if (horseshoe_tc_prepare(m, npts) != cudaSuccess) return false;
+  HsState* s = reinterpret_cast<HsState*>(m.hs_tc);
+  if (!s || !s->ok) return false;
+  P->hsf_part_gb = s->part_gb;
+  P->hsf_part_rr = s->part_rr;
+  P->hsf_bs = reinterpret_cast<uint16_t*>(s->bs);
+  P->hsf_N = m.n;
+  P->hsf_total = (int64_t)s->cp * s->kp;
+  P->hsf_P = m.p;
+  P->hsf_kp = s->kp;
+  P->hsf_splits = s->splits;
+  P->hsf_ldg = s->pp;
+  P->hsf_ld_rr = s->cp;
+  P->hsf_mtiles = s->np / TN;
+  P->hsf_nc = m.hyper[0] != 0.0;
+  return true;
+}
+
 cudaError_t horseshoe_tc_launch(ModelDev& m, const float* Q, int npts, double* PE, float* G, const int32_t* pending,
-                                cudaStream_t st) {
+                                cudaStream_t st, bool fused_tick) {
   using namespace hstc;
   HsState* s = reinterpret_cast<HsState*>(m.hs_tc);
   if (!s || !s->ok) return cudaErrorNotSupported;
   cudaError_t e = horseshoe_tc_prepare(m, npts);
   if (e != cudaSuccess) return e;
   const int cp = round_up(npts, TM), nc = m.hyper[0] != 0.0;
-  split_beta_kernel<<<std::min(1024, (cp * s->kp + 255) / 256), 256, 0, st>>>(Q, npts, m.D, m.p, nc, s->cp, s->kp,
-                                                                               s->bs, pending);
+  // In the tick engine's fused form the state-machine kernel writes the coefficient terms with the
+  // positions and finishes the potential, so only the two GEMMs run here.
+  if (!fused_tick)
+    split_beta_kernel<<<std::min(1024, (cp * s->kp + 255) / 256), 256, 0, st>>>(Q, npts, m.D, m.p, nc, s->cp, s->kp,
+                                                                                 s->bs, pending);
   GemmArgs g1{};
   g1.mode = 1;
   g1.a_rows_split = s->cp;
@@ -468,8 +493,9 @@ cudaError_t horseshoe_tc_launch(ModelDev& m, const float* Q, int npts, double* P
   g2.err = s->err;
   g2.pending = pending;
   hs_tc_gemm_kernel<<<dim3(s->pp / TN, cp / TM, s->splits), NUM_THREADS, SMEM_BYTES, st>>>(s->tm_rt, s->tm_xt, g2);
-  horseshoe_finish_launch(Q, npts, m.D, m.p, m.n, s->part_gb, s->splits, s->pp, s->part_rr, s->cp, s->np / TN, nc,
-                          PE, G, pending, st);
+  if (!fused_tick)
+    horseshoe_finish_launch(Q, npts, m.D, m.p, m.n, s->part_gb, s->splits, s->pp, s->part_rr, s->cp, s->np / TN, nc,
+                            PE, G, pending, st);
   return cudaGetLastError();
 }
 

@@ -103,8 +103,9 @@ cudaError_t measure_sfu_rate(int mode, cudaStream_t st, double* ops_per_s);
 // potentials_simt.cu: returns cudaError of the launch
 cudaError_t ensure_potential_scratch(ModelDev& m, int points);
 void free_potential_scratch(ModelDev& m);
-// fused_tick: the tick engine's call, whose advance kernel fuses the tensor-core logistic
-// potential's coefficient split and finish (logreg_tc_fusion); other potentials ignore it
+// fused_tick: the tick engine's call, whose advance kernel fuses the tensor-core logistic and
+// horseshoe potentials' coefficient split and finish (logreg_tc_fusion, horseshoe_tc_fusion);
+// other potentials ignore it
 cudaError_t launch_potential(ModelDev& m, const float* Q, int npts, double* PE, float* G,
                              const int32_t* pending, cudaStream_t st, bool fused_tick = false);
 // Times the candidate launch shapes of this model's potential at npts points (Q: any valid
@@ -123,7 +124,8 @@ void horseshoe_tc_free(ModelDev& m);
 int horseshoe_tc_error(const ModelDev& m);  // nonzero: a device wait timed out
 int* horseshoe_tc_error_ptr(const ModelDev& m);  // device address of that error word (or null)
 cudaError_t horseshoe_tc_launch(ModelDev& m, const float* Q, int npts, double* PE, float* G, const int32_t* pending,
-                                cudaStream_t st);
+                                cudaStream_t st,
+                                bool fused_tick = false);
 
 // logreg_tc.cu (tensor-core BF16 split-precision logistic potential)
 bool logreg_tc_supported(const ModelDev& m);
@@ -138,5 +140,8 @@ cudaError_t logreg_tc_launch(ModelDev& m, const float* Q, int npts, double* PE, 
 // Fills P's lrf_* fields so the tick engine's advance kernel fuses this potential's coefficient split
 // and row-group finish (launches over npts points); false when the tensor-core path is not set up.
 bool logreg_tc_fusion(const ModelDev& m, int npts, AdvParams* P);
+// the tensor-core horseshoe potential's coefficient split and finish fused into the tick engine
+// (for the CTA-per-chain state machine only)
+bool horseshoe_tc_fusion(ModelDev& m, int npts, AdvParams* P);
 
 }  // namespace gbn

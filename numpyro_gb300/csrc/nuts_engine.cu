@@ -29,6 +29,7 @@
 #include "common.cuh"
 #include "hier_potential.cuh"
 #include "internal.h"
+#include "hs_finish.cuh"
 #include "lr_finish.cuh"
 #include "sv_potential.cuh"
 
@@ -992,6 +993,14 @@ __global__ void __launch_bounds__(256) advance_kernel(const AdvParams* __restric
                          P.lrf_inv_var, P.lrf_pe_const, P.e.PE, P.e.G, tid, P.lrf_split3, P.lrf_e_tanh != 0);
     __syncwarp();  // G and PE written by other lanes
   }
+  if (NT == 256 && P.hsf_part_gb && c < P.C) {
+    // the tensor-core horseshoe potential of the previous tick ends here for a chain that queried it
+    const int ph = P.e.ctl[c].phase;
+    if (ph == PH_LEAF || ph == PH_HMC || ph == PH_HEUR)
+      horseshoe_finish_block(P.e.Q, c, P.D, P.hsf_P, P.hsf_N, P.hsf_part_gb, P.hsf_splits, P.hsf_ldg, P.C,
+                             P.hsf_part_rr, P.hsf_ld_rr, P.hsf_mtiles, P.hsf_nc, P.e.PE, P.e.G, tid, red);
+    __syncthreads();  // G and PE written by other threads
+  }
   if (c < P.C) {
     Chain<NT, DM> ch{P, Group<NT>{tid}, red, c, P.e.chain_dim ? P.e.chain_dim[c] : P.D, P.D, P.e.ctl[c], nullptr};
     ch.run();
@@ -1003,6 +1012,24 @@ __global__ void __launch_bounds__(256) advance_kernel(const AdvParams* __restric
     }
   }
   int np = __syncthreads_count(pending);
+  if (NT == 256 && P.hsf_bs && np && c < P.C) {
+    // the coefficients of the position this chain queries, as the GEMMs take them: beta (or
+    // tau lambda unscaled_beta when non-centred) split into bf16 hi/mid/lo, split_beta_kernel's
+    // arithmetic (Q is complete: the count above synchronised the CTA)
+    const float* z = P.e.Q + (size_t)c * P.D;
+    const int Pn = P.hsf_P;
+    for (int k = tid; k < Pn; k += NT) {
+      const float v = P.hsf_nc ? expf(z[Pn + 1] + z[k]) * z[Pn + 2 + k] : z[k];
+      const __nv_bfloat16 hi = __float2bfloat16_rn(v);
+      const float r1 = v - __bfloat162float(hi);
+      const __nv_bfloat16 mid = __float2bfloat16_rn(r1);
+      const __nv_bfloat16 lo = __float2bfloat16_rn(r1 - __bfloat162float(mid));
+      const size_t i = (size_t)c * P.hsf_kp + k;
+      P.hsf_bs[i] = __bfloat16_as_ushort(hi);
+      P.hsf_bs[P.hsf_total + i] = __bfloat16_as_ushort(mid);
+      P.hsf_bs[2 * P.hsf_total + i] = __bfloat16_as_ushort(lo);
+    }
+  }
   int na = __syncthreads_count(active);
   if (threadIdx.x == 0) {
     if (np) atomicAdd(&P.counters[2 * parity], np);

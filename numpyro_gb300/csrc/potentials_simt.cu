@@ -24,6 +24,7 @@
 #include "common.cuh"
 #include "hier_potential.cuh"
 #include "internal.h"
+#include "hs_finish.cuh"
 #include "lr_finish.cuh"
 #include "sv_potential.cuh"
 
@@ -348,63 +349,8 @@ __global__ void __launch_bounds__(256) horseshoe_finish_kernel(const float* __re
                                                                const int32_t* pending) {
   if (pending && *pending == 0) return;
   __shared__ double red[16];
-  const int c = blockIdx.x, tid = threadIdx.x;
-  Group<256> g{tid};
-  const float* z = Q + (size_t)c * ld;
-  float* gz = G + (size_t)c * ld;
-  const int i_sig = noncentred ? P : 2 * P, i_tau = i_sig + 1;
-  const float lsig = z[i_sig], ltau = z[i_tau];
-  const float inv_sig2 = expf(-2.0f * lsig);
-  double rrd = 0.0;  // this thread's row tiles (at most a few), then a float-float pair
-  for (int t = tid; t < mtiles; t += 256) rrd += part_rr[(size_t)t * ld_rr + c];
-  const float rr_hi = (float)rrd;
-  const FF rr_ff{rr_hi, (float)(rrd - (double)rr_hi)};
-  Comp32 lp{0.0f, 0.0f}, gt{0.0f, 0.0f};
-  for (int d = tid; d < P; d += 256) {
-    float gb = 0.0f;
-    for (int k = 0; k < splits; ++k) gb += part_gb[((size_t)k * npts + c) * ldg + d];
-    const float gx = gb * inv_sig2;  // (X^T R)_d / sigma^2
-    const float l = noncentred ? z[d] : z[P + d];
-    const float e2 = expf(-2.0f * fabsf(l));
-    const float log1p_lam2 = 2.0f * fmaxf(l, 0.0f) + log1pf(e2);
-    const float hc = (l >= 0.0f) ? 2.0f / (1.0f + e2) : 2.0f * e2 / (1.0f + e2);  // 2 lam^2 / (1 + lam^2)
-    if (noncentred) {
-      const float eta = z[P + 2 + d];
-      const float scale = expf(ltau + l);  // tau lambda_d
-      const float bg = scale * eta * gx;   // beta_d g_d
-      gz[P + 2 + d] = eta - scale * gx;
-      gz[d] = hc - 1.0f - bg;
-      lp.add(-0.5f * eta * eta - log1p_lam2 + l);
-      gt.add(-bg);
-    } else {
-      const float b = z[d];
-      const float inv_s2 = expf(-2.0f * (ltau + l));
-      const float b2s = b * b * inv_s2;
-      gz[d] = b * inv_s2 - gx;
-      gz[P + d] = hc - b2s;
-      lp.add(-0.5f * b2s - log1p_lam2);
-      gt.add(1.0f - b2s);
-    }
-  }
-  FF flp = comp_ff(lp), fgt = comp_ff(gt);
-  g.sum2ff(flp, fgt, red);
-  FF frr = g.sumff(rr_ff, red);
-  if (tid == 0) {
-    // The scalar factors come from FP32 transcendentals (correctly rounded to ~1 ulp) and are
-    // combined in FP64 where a term is large (N log sigma, RR / sigma^2): an FP64 exp or log1p on
-    // one thread costs microseconds on GB300's FP64 pipe, at the end of every chain's launch.
-    const double RR = ff_value(frr), dlsig = lsig, dltau = ltau;
-    const float sigf = expf(lsig), tauf = expf(ltau);
-    const double sig = sigf, tau = tauf, inv_s2 = inv_sig2;
-    // per coordinate: Normal(beta; 0, tau lambda) or Normal(unscaled; 0, 1), HalfCauchy(lambda; 1)
-    double total = ff_value(flp) + (double)P * (LOG_2 - LOG_PI - 0.5 * LOG_2PI - (noncentred ? 0.0 : dltau));
-    total += -0.5 * sig * sig - 0.5 * LOG_2PI + LOG_2 + dlsig;  // HalfNormal(sigma; 1) + log-det
-    total += -LOG_PI - (double)log1pf(tauf * tauf) + LOG_2 + dltau;  // HalfCauchy(tau; 1) + log-det
-    total += -0.5 * RR * inv_s2 - (double)N * dlsig - 0.5 * (double)N * LOG_2PI;
-    PE[c] = -total;
-    gz[i_sig] = (float)(sig * sig - 1.0 - RR * inv_s2 + (double)N);
-    gz[i_tau] = (float)(ff_value(fgt) + (double)(2.0f * tauf * tauf / (1.0f + tauf * tauf)) - 1.0);
-  }
+  horseshoe_finish_block(Q, blockIdx.x, ld, P, N, part_gb, splits, ldg, npts, part_rr, ld_rr, mtiles, noncentred, PE,
+                         G, threadIdx.x, red);
 }
 
 // ============================================================ stochastic volatility
@@ -539,7 +485,7 @@ cudaError_t launch_potential(ModelDev& m, const float* Q, int npts, double* PE, 
       break;
     }
     case 3: {
-      if (m.precision == 1 && m.hs_tc) return horseshoe_tc_launch(m, Q, npts, PE, G, pending, st);
+      if (m.precision == 1 && m.hs_tc) return horseshoe_tc_launch(m, Q, npts, PE, G, pending, st, fused_tick);
       const int P = m.p, M = (int)m.n, cp = pad4(npts), pp = pad4(P);
       const int tm = m.tune.hs_tm, splits = m.tune.hs_splits, bm = 16 * tm;
       const int mt = (M + bm - 1) / bm;

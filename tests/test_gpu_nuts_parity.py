@@ -242,3 +242,28 @@ def test_fused_tensor_core_tick_matches_separate_split_and_finish(monkeypatch):
         k.close()
     for a, b in zip(res[0], res[1]):
         np.testing.assert_array_equal(a, b)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("noncentered", [True, False])
+def test_fused_horseshoe_tick_matches_separate_split_and_finish(monkeypatch, noncentered):
+    """The same fusion for the tensor-core horseshoe potential, where the state machine runs a CTA
+    per chain (latent dimension > 1024; below that the warp-per-chain kernel runs and the split and
+    finish stay separate kernels): the state-machine kernel writes the coefficients' bf16 terms of
+    each queried position and finishes the previous potential (hs_finish.cuh), leaving the two
+    GEMMs as the tick's other launches.  With GBN_FUSE_TICK=0 the split and finish run as their
+    own kernels.  Bit-identical draws."""
+    X, yv, _ = datasets.horseshoe_data(seed=3, n=600, p=520, nonzero=5)
+    model = models.HorseshoeRegression(X, yv, noncentered=noncentered)
+    assert model.latent_dim > 1024
+    res = []
+    for fuse in ("1", "0"):
+        monkeypatch.setenv("GBN_FUSE_TICK", fuse)
+        k = NUTS(model, num_chains=128, precision="bf16x3")
+        st = k.init(SEED, 40)
+        out = k.run_device(st, 60, collect_start=0, collect=("z", "num_steps"))
+        res.append((out["z"].cpu().numpy(), out["num_steps"].cpu().numpy(), st.z.cpu().numpy(),
+                    st.potential_energy.cpu().numpy()))
+        k.close()
+    for a, b in zip(res[0], res[1]):
+        np.testing.assert_array_equal(a, b)
