@@ -145,7 +145,8 @@ def workload_run(w, precision=None, num_warmup=None, num_samples=None, diagnose=
         ess_note = "min over all %d models of the per-model min bulk-ESS (its %d chains), computed on the device" % (
             M, cpm)
         extra = {"median_model_min_bulk_ess": float(ess_m.median()),
-                 "models_rhat_over_1.01": int((rhat_m > 1.01).sum()), "models_rhat_over_1.05": int((rhat_m > 1.05).sum()),
+                 "models_rhat_over_1.01": int((rhat_m > 1.01).sum()),
+                 "models_rhat_over_1.05": int((rhat_m > 1.05).sum()),
                  "models": M}
         picked = list(range(0, M, 64))  # the strided sample the --diagnose comparison runs on the oracle
         worst = [int(m) for m in torch.argsort(rhat_m, descending=True)[:4].tolist()]  # and the GPU's worst
@@ -228,10 +229,12 @@ def _oracle_diagnosis(w, model, z, picked, W, S, model_rhat):
             e_o, r_o = min_bulk_ess(res["samples"][:, :, :D])
             k = len(picked) + i
             e_g, r_g = min_bulk_ess(z[4 * k:4 * k + 4, :, :D])
-            worst_rows.append({"model": int(m), "J": D - 2, "gpu_rhat": r_g, "oracle_rhat": r_o, "gpu_min_bulk_ess": e_g,
+            worst_rows.append({"model": int(m), "J": D - 2, "gpu_rhat": r_g, "oracle_rhat": r_o,
+                               "gpu_min_bulk_ess": e_g,
                                "oracle_min_bulk_ess": e_o, "oracle_divergences": int(res["diverging"].sum()),
                                "gpu_chain_sds_of_log_tau": [float(np.std(z[4 * k + j, :, 1])) for j in range(4)],
-                               "oracle_chain_sds_of_log_tau": [float(np.std(res["samples"][j, :, 1])) for j in range(4)]})
+                               "oracle_chain_sds_of_log_tau": [float(np.std(res["samples"][j, :, 1]))
+                                                               for j in range(4)]})
         out["gpu_worst_models_of_all"] = worst_rows
         g_r, g_e, o_r, o_e, o_div, rows = [], [], [], [], 0, []
         for i, m in enumerate(picked):

@@ -899,7 +899,8 @@ int gbn_time_potential(gbn_handle h, void* stream, int32_t reps, float* ms) {
 }
 
 int gbn_measure_sfu(void* stream, int32_t mode, double* ops_per_second) {
-  if (!ops_per_second || mode < 0 || mode > 2) return fail(nullptr, GBN_ERR_INVALID_ARG, "gbn_measure_sfu: bad argument");
+  if (!ops_per_second || mode < 0 || mode > 2)
+    return fail(nullptr, GBN_ERR_INVALID_ARG, "gbn_measure_sfu: bad argument");
   cudaError_t e = measure_sfu_rate(mode, (cudaStream_t)stream, ops_per_second);
   if (e != cudaSuccess) return cuda_fail(nullptr, e, "gbn_measure_sfu");
   return GBN_OK;

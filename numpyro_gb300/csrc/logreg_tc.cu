@@ -38,7 +38,8 @@
 // in its place, nu(b_hm) . b_lo (lr_finish.cuh), is exact to 1e-3: the remainder of that expansion
 // is at most (1/8) lambda_max(X^T X) |b_lo|^2 = (1/2) lambda_max |lo|^2, and the launch compares the
 // largest |lo|^2 over a block's 128 chains with 2e-3 / lambda_hat, lambda_hat a Gershgorin bound on
-// lambda_max(X^T X) formed once per model (far below the FP32 rounding of U's row sums).  The block's choice is recorded per launch (split3) for the finish.
+// lambda_max(X^T X) formed once per model (far below the FP32 rounding of U's row sums).  The
+// block's choice is recorded per launch (split3) for the finish.
 // The design matrix must be exactly representable in bf16 (checked on the host).
 // Every mbarrier wait is bounded; on a timeout the CTA records an error, drains its
 // in-flight copies and MMAs (bounded), frees TMEM and returns.

@@ -8,10 +8,11 @@ deviations).  With n comparisons (two per coordinate, up to ~1,000 here) a corre
 about 0.27 % of them beyond 3 MCSE by chance alone (some with probability 1 - 0.9973^n: 26 % for
 n = 110, 94 % for n = 1,028), so the gate asks what chance allows: at most n p3 + 3 sqrt(n p3) + 1
 comparisons beyond 3 MCSE (p3 = 0.0027), and every one within the Bonferroni bound
-Phi^-1(1 - 0.005 / n) (3.9 for n = 110, 4.4 for n = 1,028).  The oracle is the FP64 C restatement of numpyro's NUTS (oracle/nuts_ref.c),
-run on the host cores: with its own Stan warmup from init_to_uniform where that is cheap, or,
-for the logistic model, from the GPU's adapted state (its first draws are discarded, so a GPU
-posterior that were off would show as the oracle chains drifting away from it).
+Phi^-1(1 - 0.005 / n) (3.9 for n = 110, 4.4 for n = 1,028).  The oracle is the FP64 C restatement
+of numpyro's NUTS (oracle/nuts_ref.c), run on the host cores: with its own Stan warmup from
+init_to_uniform where that is cheap, or, for the logistic model, from the GPU's adapted state (its
+first draws are discarded, so a GPU posterior that were off would show as the oracle chains
+drifting away from it).  The horseshoe gate calibrates its MCSEs by two oracle runs (see there).
 
 Sizes: logistic 20,000 rows x 55 coefficients (FP32 CUDA cores and bf16x3 tensor cores),
 stochastic volatility T = 512, non-centred horseshoe N = 200, P = 50 (FP32 and bf16x3), and
