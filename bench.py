@@ -642,8 +642,8 @@ def main():
                            "logreg potential (fp32: logreg_simt_kernel + logreg_finish_kernel)"),
                 "algorithmic_flop_per_launch": flop, "launch_ms": pot_ms}
     if precision == "bf16x3":
-        # the binding pipe of the tensor-core potential: the special-function unit (ex2 + tanh per
-        # logit, one lg2 per 8 rows), against its own measured peak on this GPU
+        # the special-function unit's share of the tensor-core potential (one ex2 per logit, tanh for
+        # half the rows, one rcp and one lg2 per 8 rows), against its own measured peak on this GPU
         roofline["special_function_unit"] = _sfu_roofline(pot_ms, X.shape[0], C)
     # ---------------- end to end through the public API with host buffers
     e2e = None
