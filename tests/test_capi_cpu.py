@@ -181,3 +181,15 @@ def test_transfer_states_to_host_converts_tensors():
     m.transfer_states_to_host()
     assert isinstance(m._states["z"]["mu"], np.ndarray) and isinstance(m._states["diverging"], np.ndarray)
     assert m.get_samples()["mu"].shape == (4,)
+
+
+def test_diagnostic_entry_points_reject_null_arguments():
+    """gbn_logreg_terms and gbn_measure_sfu check their arguments before touching the GPU."""
+    from numpyro_gb300 import _lib
+
+    lib = _lib.load()
+    three, blocks, limit = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_float()
+    invalid = 1  # GBN_ERR_INVALID_ARG
+    assert lib.gbn_logreg_terms(None, ctypes.byref(three), ctypes.byref(blocks), ctypes.byref(limit)) == invalid
+    assert b"null argument" in lib.gbn_last_error(None)
+    assert lib.gbn_measure_sfu(None, 7, ctypes.byref(ctypes.c_double())) == invalid
