@@ -530,10 +530,12 @@ def run_reference(args):
     return 0
 
 
-def replica_seed(rank):
-    """Replicas: each rank runs its own chains from its own seed (chains never share a stream
-    address across ranks); nothing is exchanged during sampling."""
-    return 1000 + rank
+def replica_chains(rank, chains):
+    """Replicas: one seed for every rank, and rank r runs the global chains r C .. (r + 1) C - 1
+    (first_chain): every draw is addressed by (seed, global chain id, ...) in the counter-based
+    streams, so an N-GPU run is the single-GPU run of N C chains split by chain, chain for chain.
+    Nothing is exchanged during sampling."""
+    return 1000, rank * chains
 
 
 def reduce_over_ranks(dist, total_ms, ess, grad_evals, device="cpu"):
@@ -573,8 +575,8 @@ def main():
     X, y, _ = datasets.covtype_like(seed=0, n=args.n)
     model = models.LogisticRegression(X, y)
     C = args.chains
-    kernel = NUTS(model, num_chains=C, engine=args.engine, precision=precision)
-    seed = replica_seed(rank)
+    seed, first_chain = replica_chains(rank, C)
+    kernel = NUTS(model, num_chains=C, engine=args.engine, precision=precision, first_chain=first_chain)
     t0 = time.perf_counter()
     log("init %d chains, precision %s" % (C, precision))
     state = kernel.init(seed, args.num_warmup)

@@ -112,6 +112,11 @@ typedef struct {
    * mass matrices stay [C][D][D] (block-diagonal); at each window end the Welford covariance keeps
    * only the entries within a block and the diagonal. */
   const int32_t* mass_blocks;
+  /* Global id of the handle's chain 0 (>= 0).  Every random draw of chain c is addressed by
+   * (seed, first_chain + c, iteration, purpose) in the counter-based Philox streams, so a run split
+   * across handles or GPUs -- each with its own range of chains, one seed -- gives every chain the
+   * draws it has in one handle of all the chains. */
+  int32_t first_chain;
 } gbn_config;
 
 /* HMCState (numpyro/infer/hmc.py:31-47) + HMCAdaptState (hmc_util.py:18-30)

@@ -67,6 +67,7 @@ class Config(ctypes.Structure):
         ("init_step_size", ctypes.c_double),
         ("seed", ctypes.c_uint64),
         ("mass_blocks", c_int32_p),
+        ("first_chain", ctypes.c_int32),
     ]
 
 

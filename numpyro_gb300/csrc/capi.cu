@@ -231,6 +231,8 @@ int gbn_create(gbn_handle* out, const gbn_model_desc* md, const gbn_config* cfg)
   if (!out || !md || !cfg) return fail(nullptr, GBN_ERR_INVALID_ARG, "gbn_create: null argument");
   *out = nullptr;
   if (cfg->num_chains <= 0) return fail(nullptr, GBN_ERR_INVALID_ARG, "num_chains must be positive");
+  if (cfg->first_chain < 0 || (int64_t)cfg->first_chain + cfg->num_chains > INT32_MAX)
+    return fail(nullptr, GBN_ERR_INVALID_ARG, "first_chain must be >= 0 (with first_chain + num_chains < 2^31)");
   if (cfg->algo != GBN_ALGO_NUTS && cfg->algo != GBN_ALGO_HMC)
     return fail(nullptr, GBN_ERR_INVALID_ARG, "algo must be NUTS or HMC");
   if (cfg->max_tree_depth < 1 || cfg->max_tree_depth > 20 || cfg->max_tree_depth_warmup < 1 ||
@@ -645,7 +647,7 @@ int gbn_init(gbn_handle h, void* stream, int32_t num_warmup, const float* d_init
   refresh_fusion(h);
   e = upload_params(h, s);
   if (e != cudaSuccess) return cuda_fail(h, e, "gbn_init: params");
-  launch_set_rng_chain(st->rng_key, h->C, 0, s);
+  launch_set_rng_chain(st->rng_key, h->C, h->cfg.first_chain, s);
   int C = h->C, D = h->D;
   if (d_init_z) {
     e = cudaMemcpyAsync(st->z, d_init_z, sizeof(float) * (size_t)C * D, cudaMemcpyDeviceToDevice, s);

@@ -100,7 +100,7 @@ class HMC(MCMCKernel):
                  adapt_step_size=True, adapt_mass_matrix=True, dense_mass=False, target_accept_prob=0.8,
                  num_steps=None, trajectory_length=2 * math.pi, init_strategy=init_to_uniform,
                  find_heuristic_step_size=False, forward_mode_differentiation=False, regularize_mass_matrix=True,
-                 *, engine="fused", precision="fp32", num_chains=None):
+                 *, engine="fused", precision="fp32", num_chains=None, first_chain=0):
         if not (model is None) ^ (potential_fn is None):
             raise ValueError("Only one of `model` or `potential_fn` must be specified.")
         if potential_fn is not None:
@@ -145,6 +145,11 @@ class HMC(MCMCKernel):
         self._engine = engine
         self._precision = precision
         self._num_chains = num_chains
+        # global id of this kernel's chain 0: a run split over kernels (or GPUs), one seed and a
+        # chain range each, gives every chain the draws it has in one kernel of all the chains
+        if int(first_chain) < 0:
+            raise ValueError("first_chain must be >= 0")
+        self._first_chain = int(first_chain)
         self._handle = None
         self._handle_key = None
         self._keep = None
@@ -199,6 +204,7 @@ class HMC(MCMCKernel):
         cfg.max_delta_energy = 1000.0
         cfg.init_step_size = self._step_size
         cfg.seed = seed
+        cfg.first_chain = self._first_chain
         return cfg
 
     def _ensure_handle(self, num_chains, seed):
@@ -431,7 +437,7 @@ class NUTS(HMC):
                  adapt_step_size=True, adapt_mass_matrix=True, dense_mass=False, target_accept_prob=0.8,
                  trajectory_length=None, max_tree_depth=10, init_strategy=init_to_uniform,
                  find_heuristic_step_size=False, forward_mode_differentiation=False, regularize_mass_matrix=True,
-                 *, engine="fused", precision="fp32", num_chains=None):
+                 *, engine="fused", precision="fp32", num_chains=None, first_chain=0):
         super().__init__(model=model, potential_fn=potential_fn, kinetic_fn=kinetic_fn, step_size=step_size,
                          inverse_mass_matrix=inverse_mass_matrix, adapt_step_size=adapt_step_size,
                          adapt_mass_matrix=adapt_mass_matrix, dense_mass=dense_mass,
@@ -439,7 +445,7 @@ class NUTS(HMC):
                          init_strategy=init_strategy, find_heuristic_step_size=find_heuristic_step_size,
                          forward_mode_differentiation=forward_mode_differentiation,
                          regularize_mass_matrix=regularize_mass_matrix, engine=engine, precision=precision,
-                         num_chains=num_chains)
+                         num_chains=num_chains, first_chain=first_chain)
         self._max_tree_depth = max_tree_depth
         self._algo = "NUTS"
 

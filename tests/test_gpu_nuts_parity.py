@@ -267,3 +267,26 @@ def test_fused_horseshoe_tick_matches_separate_split_and_finish(monkeypatch, non
         k.close()
     for a, b in zip(res[0], res[1]):
         np.testing.assert_array_equal(a, b)
+
+
+@pytest.mark.gpu
+def test_chains_split_over_kernels_keep_their_draws():
+    """first_chain: every draw is addressed by (seed, global chain id, ...), so 128 chains run as two
+    kernels of 64 (global ids 0-63 and 64-127, one seed) give the draws of one kernel of 128, chain
+    for chain -- how bench.py shards replicas over GPUs."""
+    y, s = datasets.eight_schools(0)
+    model = models.HierarchicalNormal(y, s)
+    whole = NUTS(model, num_chains=128)
+    st = whole.init(SEED, 100)
+    ref = whole.run_device(st, 150, collect_start=100, collect=("z", "num_steps"))
+    ref = (ref["z"].cpu().numpy(), ref["num_steps"].cpu().numpy())
+    whole.close()
+    parts = []
+    for r in range(2):
+        k = NUTS(model, num_chains=64, first_chain=64 * r)
+        st = k.init(SEED, 100)
+        out = k.run_device(st, 150, collect_start=100, collect=("z", "num_steps"))
+        parts.append((out["z"].cpu().numpy(), out["num_steps"].cpu().numpy()))
+        k.close()
+    np.testing.assert_array_equal(np.concatenate([p[0] for p in parts]), ref[0])
+    np.testing.assert_array_equal(np.concatenate([p[1] for p in parts]), ref[1])

@@ -1,6 +1,6 @@
-"""The replica (N>1) path of bench.py on CPU: two gloo ranks, no GPU.  Chains shard across ranks
-with no data-path collective; only the final figures are reduced (max time, summed ESS and
-gradient evaluations)."""
+"""The replica (N>1) path of bench.py on CPU: two gloo ranks, no GPU.  Chains shard across ranks by
+global chain id (one seed, a chain range per rank) with no data-path collective; only the final
+figures are reduced (max time, summed ESS and gradient evaluations)."""
 import os
 import socket
 
@@ -26,7 +26,7 @@ def _rank_main(rank, world, port, out):
     try:
         # rank r pretends to have sampled for (10 + r) ms with ESS 100 (r + 1) and 1000 (r + 1) gradients
         res = bench.reduce_over_ranks(dist, 10.0 + rank, 100.0 * (rank + 1), 1000 * (rank + 1))
-        out[rank] = (res, bench.replica_seed(rank))
+        out[rank] = (res, bench.replica_chains(rank, 1024))
     finally:
         dist.destroy_process_group()
 
@@ -41,4 +41,5 @@ def test_two_gloo_ranks_reduce_like_the_bench():
     for rank in range(world):
         (ms, ess, grads), seed = res[rank]
         assert ms == 11.0 and ess == 300.0 and grads == 3000
-    assert res[0][1] != res[1][1]  # independent streams per rank
+    # one seed, disjoint global chain ranges: the ranks' chains are the single run's, split by chain
+    assert res[0][1] == (1000, 0) and res[1][1] == (1000, 1024)
