@@ -687,7 +687,7 @@ def main():
         "data": "synthetic", "impl": "ours",
         "config": {"workload": WORKLOAD, "chains": C, "n": X.shape[0], "d": X.shape[1], "engine": args.engine,
                    "precision": precision, "iters_per_step": B, "l2": "flushed (512 MB write) before each step",
-                   "parallelism": "replicas" if world > 1 else "single"},
+                   "parallelism": "replicas, chains sharded by global chain id" if world > 1 else "single"},
         "grad_evals_per_s": grad_evals / (total_ms / 1e3),
         "min_bulk_ess": ess, "rhat_max": rhat, "warmup_s": warmup_ms / 1e3,
         "setup_s": time.perf_counter() - t0,
